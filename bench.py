@@ -1,0 +1,465 @@
+"""Benchmark of the GB300 sort/select library (one JSON line on stdout).
+
+python bench.py [--gpus N] [--steps K] [--warmup W] [--workload NAME] [--impl ours|reference]
+
+Default workload: keyvalue_qsort of 2^28 int64 keys (uniform over the full
+range) carrying uint64 values = original index, ascending -- the key-value
+half of the reference's 2^28 configuration.  A step is one sort of the whole
+array; the input is restored from a pristine device copy before every step,
+outside the timed events (as the reference's benchmarks restore outside
+PauseTiming, benchmarks/bench-qsort.hpp:31-36).  Inputs (4 GiB) are far larger
+than L2, so no flush is needed between steps.
+
+`value` is device-resident throughput (Gkeys/s, CUDA events on the launching
+stream); `e2e` is the same sort through the host-pointer C ABI
+(xss_keyvalue_qsort) from pinned host buffers, copies included; `roofline`
+covers the dominant kernel (one onesweep radix pass) with its algorithmic
+bytes per launch; `cpu_baseline` times the CPU oracle port (or the reference
+library where it builds) on a bounded sample of the same workload.
+
+Several ranks (torchrun) run independent replicas: a single array does not
+shard without an all-to-all exchange, so each GPU sorts its own array and
+`value` is the sum over ranks of keys sorted per unit of the slowest rank's
+time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "x86-simd-sort_gb300")
+sys.path.insert(0, PKG)
+sys.path.insert(0, ROOT)
+
+
+# ---------------------------------------------------------------------------
+def _peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def _traffic(workload):
+    p = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            return json.load(f).get(workload)
+    return None
+
+
+class Clocks:
+    """nvidia-smi samples (SM clock, throttle reasons) during the timed region."""
+
+    Q = ("clocks.sm,clocks.max.sm,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.rows = []
+        self.proc = None
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(index), f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) == 6:
+                self.rows.append(parts)
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        rows = [r for r in self.rows if r[0].isdigit()]
+        if not rows:
+            return None
+        sm = [int(r[0]) for r in rows]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[2 + i] == "Active"})
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": int(rows[0][1]),
+                "reasons": reasons, "samples": len(rows)}
+
+
+# ---------------------------------------------------------------------------
+class Workload:
+    """One device-resident sort/select workload."""
+
+    dominant = "onesweep"
+
+    def __init__(self, torch, xss, n, stream):
+        self.torch, self.xss, self.n, self.stream = torch, xss, n, stream
+
+
+class KeyValueSort(Workload):
+    name = "keyvalue_qsort"
+    kdt, vdt, kb, vb = "int64", "uint64", 8, 8
+
+    def describe(self):
+        return {"workload": f"keyvalue_qsort int64->uint64 n=2^{self.n.bit_length() - 1} "
+                            "uniform full-range keys, values=index, ascending",
+                "n": self.n, "l2": "inputs (4 GiB) larger than L2; input restored per step"}
+
+    def setup(self):
+        t, n = self.torch, self.n
+        g = t.Generator(device="cuda").manual_seed(1)
+        self.k0 = t.randint(0, 256, (n * 8,), dtype=t.uint8, device="cuda",
+                            generator=g).view(t.int64)
+        self.v0 = t.arange(n, dtype=t.int64, device="cuda")
+        self.k = t.empty_like(self.k0)
+        self.v = t.empty_like(self.v0)
+        self.wsb = self.xss.workspace_size("keyvalue_qsort", self.kdt, n, val_dtype=self.vdt)
+        self.ws = t.empty(max(self.wsb, 1), dtype=t.uint8, device="cuda")
+
+    def restore(self):
+        self.k.copy_(self.k0)
+        self.v.copy_(self.v0)
+
+    def run(self):
+        self.xss.gpu_keyvalue_qsort(self.kdt, self.vdt, self.k.data_ptr(), self.v.data_ptr(),
+                                    self.n, False, False, self.ws.data_ptr(), self.wsb,
+                                    self.stream.cuda_stream)
+
+    def check(self):
+        t = self.torch
+        k, v = self.k, self.v
+        ok = bool((k[1:] >= k[:-1]).all())
+        ok &= bool((self.k0[v] == k).all())
+        cnt = t.zeros(self.n, dtype=t.int32, device="cuda")
+        cnt.index_add_(0, v, t.ones(self.n, dtype=t.int32, device="cuda"))
+        ok &= bool((cnt == 1).all())
+        return ok
+
+    def passes(self):
+        return self.kb
+
+    def bytes_per_pass(self):           # read + write of key and value
+        return 2 * self.n * (self.kb + self.vb)
+
+    def bytes_model(self):              # survey model: n(kb + 2P(kb+vb))
+        return self.n * (self.kb + 2 * self.passes() * (self.kb + self.vb))
+
+    # host-pointer (e2e) path
+    def host_setup(self):
+        t = self.torch
+        self.hk0 = self.k0.cpu().numpy()
+        self.hv0 = self.v0.cpu().numpy().view(np.uint64)
+        self.hk = t.empty(self.n, dtype=t.int64, pin_memory=True).numpy()
+        self.hv = t.empty(self.n, dtype=t.int64, pin_memory=True).numpy().view(np.uint64)
+
+    def host_restore(self):
+        np.copyto(self.hk, self.hk0)
+        np.copyto(self.hv, self.hv0)
+
+    def host_run(self):
+        self.xss.keyvalue_qsort(self.hk, self.hv)
+
+    def host_bytes(self):
+        return self.n * (self.kb + self.vb), self.n * (self.kb + self.vb)
+
+    # CPU baseline on a bounded sample
+    def cpu_sample(self, m):
+        rng = np.random.default_rng(1)
+        return (rng.integers(np.iinfo(np.int64).min, np.iinfo(np.int64).max, m, dtype=np.int64),
+                np.arange(m, dtype=np.uint64))
+
+    def cpu_run(self, lib, kind, sample, threads):
+        k, v = sample[0].copy(), sample[1].copy()
+        if kind == "reference":
+            rc = lib.keyvalue_qsort(7, 6, k.ctypes.data, v.ctypes.data, k.size, 0, 0)
+        else:
+            rc = lib.keyvalue_qsort_mt(7, 6, k.ctypes.data, v.ctypes.data, k.size, 0, 0, threads)
+        assert rc == 0
+
+
+class QsortF32(Workload):
+    name = "qsort_f32"
+    kb = 4
+
+    def describe(self):
+        return {"workload": f"qsort float32 n=2^{self.n.bit_length() - 1} uniform [-1,1), "
+                            "ascending, hasnan=false", "n": self.n,
+                "l2": "inputs larger than L2; input restored per step"}
+
+    def setup(self):
+        t = self.torch
+        g = t.Generator(device="cuda").manual_seed(0)
+        self.k0 = t.rand(self.n, dtype=t.float32, device="cuda", generator=g) * 2 - 1
+        self.k = t.empty_like(self.k0)
+        self.wsb = self.xss.workspace_size("qsort", "float32", self.n)
+        self.ws = t.empty(max(self.wsb, 1), dtype=t.uint8, device="cuda")
+
+    def restore(self):
+        self.k.copy_(self.k0)
+
+    def run(self):
+        self.xss.gpu_qsort("float32", self.k.data_ptr(), self.n, False, False,
+                           self.ws.data_ptr(), self.wsb, self.stream.cuda_stream)
+
+    def check(self):
+        k = self.k
+        ok = bool((k[1:] >= k[:-1]).all())
+        ok &= bool((self.torch.sort(self.k0).values == k).all())
+        return ok
+
+    def passes(self):
+        return 4
+
+    def bytes_per_pass(self):
+        return 2 * self.n * self.kb
+
+    def bytes_model(self):
+        return self.n * self.kb * (1 + 2 * self.passes())
+
+    def host_setup(self):
+        self.hk0 = self.k0.cpu().numpy()
+        self.hk = self.torch.empty(self.n, dtype=self.torch.float32, pin_memory=True).numpy()
+
+    def host_restore(self):
+        np.copyto(self.hk, self.hk0)
+
+    def host_run(self):
+        self.xss.qsort(self.hk)
+
+    def host_bytes(self):
+        return self.n * 4, self.n * 4
+
+    def cpu_sample(self, m):
+        return (np.random.default_rng(0).random(m, dtype=np.float32) * 2 - 1,)
+
+    def cpu_run(self, lib, kind, sample, threads):
+        k = sample[0].copy()
+        if kind == "reference":
+            rc = lib.qsort(5, k.ctypes.data, k.size, 0, 0)
+        else:
+            rc = lib.qsort_mt(5, k.ctypes.data, k.size, 0, 0, threads)
+        assert rc == 0
+
+
+WORKLOADS = {"keyvalue_qsort": (KeyValueSort, 1 << 28), "qsort_f32": (QsortF32, 1 << 28)}
+
+
+# ---------------------------------------------------------------------------
+def cpu_baseline(wl, budget_s=12.0, sample_n=1 << 24):
+    """Time the reference (where it builds here) or the oracle's port on a sample."""
+    from oracle import pyoracle
+    lib, kind = pyoracle.reference(), "reference"
+    if lib is None:
+        lib, kind = pyoracle.oracle(), "port"
+    threads = pyoracle.oracle().max_threads()
+    sample = wl.cpu_sample(sample_n)
+    times = []
+    t_end = time.perf_counter() + budget_s
+    while time.perf_counter() < t_end or len(times) < 2:
+        t0 = time.perf_counter()
+        wl.cpu_run(lib, kind, sample, threads)
+        times.append(time.perf_counter() - t0)
+        if len(times) >= 10:
+            break
+    med = statistics.median(times)
+    return {"value": sample_n / med / 1e9, "unit": "Gkeys/s", "cores": threads if kind == "port"
+            else min(16, os.cpu_count() or 1), "kind": kind,
+            "sample": f"{wl.name} on {sample_n} keys (2^{sample_n.bit_length() - 1}), "
+                      f"median of {len(times)} runs"}
+
+
+def reference_arm(args):
+    """--impl reference: the reference's CPU path on bounded samples of the workload."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    import torch  # noqa: F401  (only for the workload class' sample helpers)
+    cls, n_full = WORKLOADS[args.workload]
+    wl = cls(None, None, n_full, None)
+    from oracle import pyoracle
+    lib, kind = pyoracle.reference(), "reference"
+    if lib is None:
+        lib, kind = pyoracle.oracle(), "port"
+    threads = pyoracle.oracle().max_threads()
+    m = args.cpu_sample
+    sample = wl.cpu_sample(m)
+    for _ in range(args.warmup):
+        wl.cpu_run(lib, kind, sample, threads)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        wl.cpu_run(lib, kind, sample, threads)
+    dt = time.perf_counter() - t0
+    val = m * args.steps / dt / 1e9
+    line = {"impl": "reference", "metric": "Gkeys/s", "value": val, "unit": "Gkeys/s",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": dt / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": wl.describe_dtype() if hasattr(wl, "describe_dtype")
+            else ("int64" if args.workload == "keyvalue_qsort" else "f32"),
+            "data": "synthetic",
+            "config": {"workload": f"{args.workload} (bounded CPU sample of {m} keys)",
+                       "full_n": n_full},
+            "cpu_baseline": {"value": val, "unit": "Gkeys/s",
+                             "cores": threads if kind == "port" else min(16, os.cpu_count() or 1),
+                             "kind": kind, "sample": f"{m} keys per step"},
+            "e2e": {"value": val, "unit": "Gkeys/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--workload", default="keyvalue_qsort", choices=sorted(WORKLOADS))
+    ap.add_argument("--n", type=int, default=0, help="override the array size")
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--cpu-sample", type=int, default=1 << 24)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    args = ap.parse_args()
+    assert args.warmup >= 3 or args.impl == "reference", "at least 3 warm-up steps"
+
+    if args.impl == "reference":
+        reference_arm(args)
+        return
+
+    import torch
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+
+    import pyxss as xss
+    xss.lib()
+    cls, n_full = WORKLOADS[args.workload]
+    n = args.n or n_full
+    stream = torch.cuda.Stream()
+    wl = cls(torch, xss, n, stream)
+    with torch.cuda.stream(stream):
+        wl.setup()
+    torch.cuda.synchronize()
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    for _ in range(args.warmup):
+        with torch.cuda.stream(stream):
+            wl.restore()
+            wl.run()
+    xss.stream_status(stream.cuda_stream)
+
+    xss.prof_enable(True)
+    xss.prof_reset()
+    launches0 = xss.prof_launches()
+    clocks = Clocks(local)
+    barrier()
+    total_ms = 0.0
+    t_wall = time.perf_counter()
+    for _ in range(args.steps):
+        with torch.cuda.stream(stream):
+            wl.restore()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        with torch.cuda.stream(stream):
+            wl.run()
+        e1.record(stream)
+        e1.synchronize()
+        total_ms += e0.elapsed_time(e1)
+    barrier()
+    wall = time.perf_counter() - t_wall
+    clk = clocks.stop()
+    launches = xss.prof_launches() - launches0
+    dom_ms, dom_launches = xss.prof_read(wl.dominant)
+    xss.prof_enable(False)
+    xss.stream_status(stream.cuda_stream)
+    checked = wl.check()
+
+    if dist is not None:
+        tt = torch.tensor([total_ms], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        total_ms = float(tt.item())
+
+    ms_per_step = total_ms / args.steps
+    value = world * n / (ms_per_step / 1e3) / 1e9
+
+    peak, peak_src = _peaks()
+    active = dom_launches / args.steps if dom_launches else 0
+    avg_pass_ms = dom_ms / dom_launches if dom_launches else float("nan")
+    achieved = wl.bytes_per_pass() / (avg_pass_ms / 1e3) / 1e9 if dom_launches else None
+    traffic = _traffic(args.workload)
+
+    e2e = None
+    if not args.no_e2e and rank == 0:
+        wl.host_setup()
+        for _ in range(1):
+            wl.host_restore()
+            wl.host_run()
+        t = 0.0
+        for _ in range(args.steps):
+            wl.host_restore()
+            t0 = time.perf_counter()
+            wl.host_run()
+            t += time.perf_counter() - t0
+        bi, bo = wl.host_bytes()
+        e2e = {"value": n * args.steps / t / 1e9, "unit": "Gkeys/s", "h2d_bytes_per_step": bi,
+               "d2h_bytes_per_step": bo, "ms_per_step": t / args.steps * 1e3}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(wl, sample_n=args.cpu_sample)
+
+    if rank == 0:
+        line = {
+            "metric": "Gkeys/s", "value": value, "unit": "Gkeys/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": {"keyvalue_qsort": "int64", "qsort_f32": "f32"}[args.workload],
+            "data": "synthetic (seeded, generated on device)",
+            "config": {**wl.describe(), "parallelism": f"replicas x{world}"},
+            "roofline": {"bound": "hbm", "kernel": "onesweep radix pass",
+                         "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": (achieved / peak) if achieved else None,
+                         "peak_source": peak_src,
+                         "alg_bytes_per_launch": wl.bytes_per_pass(),
+                         "avg_launch_ms": avg_pass_ms, "launches_per_step": active,
+                         "traffic": traffic,
+                         "sort_model_bytes": wl.bytes_model(),
+                         "sort_frac": wl.bytes_model() / (ms_per_step / 1e3) / 1e9 / peak},
+            "e2e": e2e,
+            "cpu_baseline": cpu,
+            "gpu_launches": launches,
+            "clocks": clk,
+            "checked": checked,
+            "wall_s_timed_region": wall,
+        }
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

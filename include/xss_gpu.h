@@ -1,0 +1,182 @@
+/*
+ * xss_gpu.h -- C ABI of the GB300 sort/select library (libxss_gb300.so).
+ *
+ * Every entry point takes plain pointers and sizes.  Device-pointer entry
+ * points (xss_gpu_*) run asynchronously on the caller's stream; host-pointer
+ * entry points (xss_*) stage through device memory and return when the
+ * result is back in the caller's buffers.
+ *
+ * Semantics follow the reference library intel/x86-simd-sort:
+ *   - ordering: integers by value; floats with NaN after +inf (ascending) or
+ *     before it (descending), -0.0 and +0.0 adjacent (utils/custom-compare.h:11-34);
+ *   - qsort with hasnan writes the canonical quiet NaN into the NaN slots
+ *     (src/xss-common-qsort.h:107-135; _Float16 uses bits 0x7c01,
+ *     src/xss-custom-float.h:81-85);
+ *   - keyvalue / argsort / select keep NaN payload bits;
+ *   - k counts from the front of the requested order (descending included).
+ * Sorts are unstable, as in the reference.
+ */
+#ifndef XSS_GPU_H
+#define XSS_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Same handle type as cudaStream_t; NULL is the legacy default stream. */
+typedef struct CUstream_st *xss_stream_t;
+
+/* Status codes returned by every int-returning entry point. */
+enum {
+    XSS_OK = 0,
+    XSS_EINVAL = 1,      /* bad dtype / k >= n / null pointer with n > 1 */
+    XSS_ENOMEM = 2,      /* workspace too small or device allocation failed */
+    XSS_ETIMEOUT = 3,    /* a bounded device-side wait gave up (result invalid) */
+    XSS_ECUDA = 4,       /* a CUDA runtime call failed */
+    XSS_EUNSUPPORTED = 5,/* type combination the reference does not offer */
+    XSS_ETOOBIG = 6      /* n above the library limit (XSS_MAX_N) */
+};
+
+/* Largest array the device kernels accept (tile look-back counters are 30-bit). */
+#define XSS_MAX_N ((size_t)((1u << 30) - 1))
+
+/* Key / value element types (the reference's nine key types). */
+enum {
+    XSS_DT_U16 = 0, XSS_DT_I16 = 1, XSS_DT_F16 = 2,
+    XSS_DT_U32 = 3, XSS_DT_I32 = 4, XSS_DT_F32 = 5,
+    XSS_DT_U64 = 6, XSS_DT_I64 = 7, XSS_DT_F64 = 8
+};
+
+/* Operation ids for xss_gpu_workspace_size. */
+enum {
+    XSS_OP_QSORT = 0, XSS_OP_QSELECT = 1, XSS_OP_PARTIAL_QSORT = 2,
+    XSS_OP_ARGSORT = 3, XSS_OP_ARGSELECT = 4,
+    XSS_OP_KV_QSORT = 5, XSS_OP_KV_SELECT = 6, XSS_OP_KV_PARTIAL_SORT = 7
+};
+
+const char *xss_strerror(int status);
+/* Library version string. */
+const char *xss_version(void);
+
+/*
+ * Bytes of device scratch the call (op, key dtype, value dtype, n, k) needs.
+ * val_dtype is ignored for ops without values.  Passing d_ws = NULL to a
+ * device entry point makes the library use its own cached per-stream
+ * workspace instead (grown on demand, never shrunk).
+ */
+size_t xss_gpu_workspace_size(int op, int key_dtype, int val_dtype, size_t n, size_t k);
+
+/*
+ * Device-pointer calls are asynchronous.  Kernels that give up a bounded wait
+ * latch an error word on the device; this call synchronises `stream`, reads
+ * and clears that word and returns XSS_OK, XSS_ETIMEOUT or XSS_ECUDA.
+ */
+int xss_gpu_stream_status(xss_stream_t stream);
+
+/* ------------------------------------------------------------------ */
+/* Device-pointer entry points.  Arrays live in device memory; work is   */
+/* enqueued on `stream`; the status of bounded waits is checked with a  */
+/* small device->host read at the end of the call (the call syncs the   */
+/* stream only for that read).                                          */
+/* ------------------------------------------------------------------ */
+
+/* x86simdsort::qsort (lib/x86simdsort.h:15-18) */
+int xss_gpu_qsort(int dtype, void *d_arr, size_t n, int hasnan, int descending,
+                  void *d_ws, size_t ws_bytes, xss_stream_t stream);
+/* x86simdsort::qselect (lib/x86simdsort.h:20-26) */
+int xss_gpu_qselect(int dtype, void *d_arr, size_t k, size_t n, int hasnan,
+                    int descending, void *d_ws, size_t ws_bytes, xss_stream_t stream);
+/* x86simdsort::partial_qsort (lib/x86simdsort.h:28-34) */
+int xss_gpu_partial_qsort(int dtype, void *d_arr, size_t k, size_t n, int hasnan,
+                          int descending, void *d_ws, size_t ws_bytes,
+                          xss_stream_t stream);
+/* x86simdsort::argsort (lib/x86simdsort.h:36-39); d_arg receives n indices. */
+int xss_gpu_argsort(int dtype, const void *d_arr, uint64_t *d_arg, size_t n,
+                    int hasnan, int descending, void *d_ws, size_t ws_bytes,
+                    xss_stream_t stream);
+/* x86simdsort::argselect (lib/x86simdsort.h:41-44); no descending form. */
+int xss_gpu_argselect(int dtype, const void *d_arr, uint64_t *d_arg, size_t k,
+                      size_t n, int hasnan, void *d_ws, size_t ws_bytes,
+                      xss_stream_t stream);
+/* x86simdsort::keyvalue_qsort (lib/x86simdsort.h:46-52); 32/64-bit keys and values. */
+int xss_gpu_keyvalue_qsort(int key_dtype, int val_dtype, void *d_keys, void *d_vals,
+                           size_t n, int hasnan, int descending, void *d_ws,
+                           size_t ws_bytes, xss_stream_t stream);
+/* x86simdsort::keyvalue_select (lib/x86simdsort.h:54-61) */
+int xss_gpu_keyvalue_select(int key_dtype, int val_dtype, void *d_keys, void *d_vals,
+                            size_t k, size_t n, int hasnan, int descending,
+                            void *d_ws, size_t ws_bytes, xss_stream_t stream);
+/* x86simdsort::keyvalue_partial_sort (lib/x86simdsort.h:63-70) */
+int xss_gpu_keyvalue_partial_sort(int key_dtype, int val_dtype, void *d_keys,
+                                  void *d_vals, size_t k, size_t n, int hasnan,
+                                  int descending, void *d_ws, size_t ws_bytes,
+                                  xss_stream_t stream);
+
+/*
+ * Batched segmented sort: sorts each segment [offsets[i], offsets[i+1]) of
+ * d_keys (and d_vals when non-NULL) independently, in one launch sequence.
+ * d_offsets holds num_segments+1 non-decreasing uint64 offsets in device
+ * memory; h_offsets is the same array in host memory (used to bin segments
+ * by size on the host; may be NULL, then it is read back from the device).
+ */
+int xss_gpu_segmented_sort(int key_dtype, int val_dtype, void *d_keys, void *d_vals,
+                           const uint64_t *d_offsets, const uint64_t *h_offsets,
+                           size_t num_segments, int hasnan, int descending,
+                           void *d_ws, size_t ws_bytes, xss_stream_t stream);
+size_t xss_gpu_segmented_workspace_size(int key_dtype, int val_dtype,
+                                        const uint64_t *h_offsets,
+                                        size_t num_segments);
+
+/* ------------------------------------------------------------------ */
+/* Instrumentation: per-kernel-kind launch counts (always on) and       */
+/* optional CUDA-event timing of every launch on its own stream.        */
+/* Kinds: 0 hist, 1 onesweep pass, 2 fixup, 3 small sort, 4 select      */
+/* histogram, 5 select find, 6 partition collect, 7 partition place,    */
+/* 8 segmented small, 9 segmented block, 10 segmented bookkeeping.      */
+/* ------------------------------------------------------------------ */
+void xss_prof_enable(int on);
+void xss_prof_reset(void);
+int xss_prof_read(int kind, double *total_ms, unsigned long long *timed_launches);
+unsigned long long xss_prof_launches(int kind);
+const char *xss_prof_kind_name(int kind);
+
+/* ------------------------------------------------------------------ */
+/* Host-pointer entry points: copy in, run on the device, copy back.     */
+/* ------------------------------------------------------------------ */
+int xss_qsort(int dtype, void *arr, size_t n, int hasnan, int descending);
+int xss_qselect(int dtype, void *arr, size_t k, size_t n, int hasnan, int descending);
+int xss_partial_qsort(int dtype, void *arr, size_t k, size_t n, int hasnan,
+                      int descending);
+int xss_argsort(int dtype, const void *arr, uint64_t *arg, size_t n, int hasnan,
+                int descending);
+int xss_argselect(int dtype, const void *arr, uint64_t *arg, size_t k, size_t n,
+                  int hasnan);
+int xss_keyvalue_qsort(int key_dtype, int val_dtype, void *keys, void *vals,
+                       size_t n, int hasnan, int descending);
+int xss_keyvalue_select(int key_dtype, int val_dtype, void *keys, void *vals,
+                        size_t k, size_t n, int hasnan, int descending);
+int xss_keyvalue_partial_sort(int key_dtype, int val_dtype, void *keys, void *vals,
+                              size_t k, size_t n, int hasnan, int descending);
+
+/* ------------------------------------------------------------------ */
+/* The reference's own C symbols (lib/x86simdsort.cpp:298-339): host    */
+/* pointers, ascending, hasnan = true.  Errors abort with a message, as */
+/* the reference has no error channel here.                             */
+/* ------------------------------------------------------------------ */
+void keyvalue_qsort_float_uint32(float *key, uint32_t *val, size_t size);
+void keyvalue_qsort_float_uint64(float *key, uint64_t *val, size_t size);
+void keyvalue_qsort_uint64_uint32(uint64_t *key, uint32_t *val, size_t size);
+void keyvalue_qsort_uint64_uint64(uint64_t *key, uint64_t *val, size_t size);
+void keyvalue_qsort_int32_uint32(int32_t *key, uint32_t *val, size_t size);
+void keyvalue_qsort_int32_uint64(int32_t *key, uint64_t *val, size_t size);
+void keyvalue_qsort_uint32_uint32(uint32_t *key, uint32_t *val, size_t size);
+void keyvalue_qsort_uint32_uint64(uint32_t *key, uint64_t *val, size_t size);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* XSS_GPU_H */

@@ -1,0 +1,100 @@
+// xss_internal.cuh -- declarations shared by the kernel translation units.
+#pragma once
+#include <cstddef>
+#include <cstdint>
+#include <cuda_runtime.h>
+#include "xss_keys.cuh"
+#include "xss_prof.cuh"
+#include "../../include/xss_gpu.h"
+
+namespace xss {
+
+// Operation families understood by the sort engine.
+enum SortOp : int { SOP_KEYS = 0, SOP_KV = 1, SOP_ARG = 2 };
+
+constexpr int RADIX_BITS = 8;
+constexpr int RADIX = 1 << RADIX_BITS;
+constexpr int MAX_PASSES = 8;
+constexpr uint32_t FLAG_AGG = 1u << 30;     // tile aggregate published
+constexpr uint32_t FLAG_PRE = 2u << 30;     // inclusive prefix published
+constexpr uint32_t FLAG_MASK = 3u << 30;
+constexpr uint32_t COUNT_MASK = (1u << 30) - 1;
+
+// Inputs up to this size are sorted by one CTA in shared memory.
+constexpr size_t SMALL_SORT_MAX = 4096;
+
+// Per-pass plan written on the device by the histogram kernel.
+struct PassDesc {
+    int active;      // 0: every key has the same digit -> pass skipped
+    int src, dst;    // key buffer ids (0 = caller array, 1/2 = scratch)
+    int vsrc, vdst;  // value buffer ids
+    int first;       // load applies the key transform
+    int last;        // store applies the inverse transform
+    int gen_idx;     // values are the element index (argsort, first pass)
+    int skip_keys;   // keys are not stored (argsort, last pass)
+    int out_idx;     // values go to the 64-bit index output (argsort, last pass)
+};
+
+enum FixupMode : int { FIX_NONE = 0, FIX_COPY = 1, FIX_CANON = 2, FIX_IOTA = 3 };
+
+struct RadixHeader {
+    uint32_t hist[MAX_PASSES][RADIX];
+    uint32_t start[MAX_PASSES][RADIX];
+    PassDesc desc[MAX_PASSES];
+    uint32_t tile_ctr[MAX_PASSES];
+    uint32_t done_ctr;
+    int fixup;
+    int num_active;
+    int pad;
+};
+
+struct RadixArgs {
+    void *kbuf[3];
+    void *vbuf[3];
+    uint64_t *out_idx;
+    size_t n;
+    uint32_t num_tiles;
+    int passes;
+    int op;
+    KeyXform xf;
+    RadixHeader *hdr;
+    uint32_t *status;      // [passes][num_tiles][RADIX]
+    unsigned *err;         // device-visible error word
+};
+
+inline size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+// Device-visible error word (mapped pinned host memory); see xss_capi.cu.
+unsigned *device_error_word();
+
+// ---- launchers (defined in the .cu files) --------------------------------
+size_t radix_workspace_bytes(int op, int kbytes, int vbytes, size_t n);
+int radix_sort(int op, int kbytes, KeyXform xf, void *keys, void *vals, int vbytes,
+               uint64_t *out_idx, size_t n, void *ws, size_t ws_bytes, cudaStream_t s);
+
+size_t select_workspace_bytes(int op, int kbytes, int vbytes, size_t n);
+// Partition so that position k holds the k-th element in code order,
+// smaller codes before it and larger after.  keys are modified in place for
+// SOP_KEYS / SOP_KV; for SOP_ARG keys are read-only and out_idx receives the
+// partitioned index permutation.
+int radix_select(int op, int kbytes, KeyXform xf, void *keys, void *vals, int vbytes,
+                 uint64_t *out_idx, size_t k, size_t n, void *ws, size_t ws_bytes,
+                 cudaStream_t s);
+
+int num_sms();
+
+}  // namespace xss
+
+// Launch bracketed by the profiler hooks (launch count, optional event timing).
+#define XSS_LAUNCH(kind, stream, ...)      \
+    do {                                    \
+        ::xss::prof_begin(stream, kind);    \
+        __VA_ARGS__;                        \
+        ::xss::prof_end(stream, kind);      \
+    } while (0)
+
+#define XSS_CUDA_TRY(expr)                                  \
+    do {                                                    \
+        cudaError_t _e = (expr);                            \
+        if (_e != cudaSuccess) return XSS_ECUDA;            \
+    } while (0)

@@ -1,0 +1,261 @@
+"""ctypes binding of libxss_gb300.so, mirroring x86simdsort's API.
+
+Host-array functions take NumPy arrays and work in place, with the reference's
+names, argument order and defaults (lib/x86simdsort.h:15-70): ``qsort``,
+``qselect``, ``partial_qsort``, ``argsort``, ``argselect``, ``keyvalue_qsort``,
+``keyvalue_select``, ``keyvalue_partial_sort``.  Device functions (``gpu_*``)
+take raw device pointers (ints) plus a dtype name, or torch CUDA tensors, and
+run asynchronously on the given stream.
+
+There is no CPU fallback: if the shared library is missing, importing works
+but every call raises ``RuntimeError``.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+PKG_DIR = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG_DIR, "libxss_gb300.so")
+
+DTYPES = {
+    "uint16": 0, "int16": 1, "float16": 2,
+    "uint32": 3, "int32": 4, "float32": 5,
+    "uint64": 6, "int64": 7, "float64": 8,
+}
+KEY_BYTES = {0: 2, 1: 2, 2: 2, 3: 4, 4: 4, 5: 4, 6: 8, 7: 8, 8: 8}
+OPS = {"qsort": 0, "qselect": 1, "partial_qsort": 2, "argsort": 3, "argselect": 4,
+       "keyvalue_qsort": 5, "keyvalue_select": 6, "keyvalue_partial_sort": 7}
+STATUS = {0: "ok", 1: "EINVAL", 2: "ENOMEM", 3: "ETIMEOUT", 4: "ECUDA",
+          5: "EUNSUPPORTED", 6: "ETOOBIG"}
+
+
+class XssError(RuntimeError):
+    def __init__(self, code: int, what: str):
+        super().__init__(f"{what}: {STATUS.get(code, code)}")
+        self.code = code
+
+
+_lib = None
+
+_P = ctypes.c_void_p
+_Z = ctypes.c_size_t
+_I = ctypes.c_int
+_SIGS = {
+    "xss_strerror": (ctypes.c_char_p, [_I]),
+    "xss_version": (ctypes.c_char_p, []),
+    "xss_gpu_workspace_size": (_Z, [_I, _I, _I, _Z, _Z]),
+    "xss_gpu_stream_status": (_I, [_P]),
+    "xss_gpu_qsort": (_I, [_I, _P, _Z, _I, _I, _P, _Z, _P]),
+    "xss_gpu_qselect": (_I, [_I, _P, _Z, _Z, _I, _I, _P, _Z, _P]),
+    "xss_gpu_partial_qsort": (_I, [_I, _P, _Z, _Z, _I, _I, _P, _Z, _P]),
+    "xss_gpu_argsort": (_I, [_I, _P, _P, _Z, _I, _I, _P, _Z, _P]),
+    "xss_gpu_argselect": (_I, [_I, _P, _P, _Z, _Z, _I, _P, _Z, _P]),
+    "xss_gpu_keyvalue_qsort": (_I, [_I, _I, _P, _P, _Z, _I, _I, _P, _Z, _P]),
+    "xss_gpu_keyvalue_select": (_I, [_I, _I, _P, _P, _Z, _Z, _I, _I, _P, _Z, _P]),
+    "xss_gpu_keyvalue_partial_sort": (_I, [_I, _I, _P, _P, _Z, _Z, _I, _I, _P, _Z, _P]),
+    "xss_gpu_segmented_sort": (_I, [_I, _I, _P, _P, _P, _P, _Z, _I, _I, _P, _Z, _P]),
+    "xss_gpu_segmented_workspace_size": (_Z, [_I, _I, _P, _Z]),
+    "xss_qsort": (_I, [_I, _P, _Z, _I, _I]),
+    "xss_qselect": (_I, [_I, _P, _Z, _Z, _I, _I]),
+    "xss_partial_qsort": (_I, [_I, _P, _Z, _Z, _I, _I]),
+    "xss_argsort": (_I, [_I, _P, _P, _Z, _I, _I]),
+    "xss_argselect": (_I, [_I, _P, _P, _Z, _Z, _I]),
+    "xss_keyvalue_qsort": (_I, [_I, _I, _P, _P, _Z, _I, _I]),
+    "xss_keyvalue_select": (_I, [_I, _I, _P, _P, _Z, _Z, _I, _I]),
+    "xss_keyvalue_partial_sort": (_I, [_I, _I, _P, _P, _Z, _Z, _I, _I]),
+    "xss_prof_enable": (None, [_I]),
+    "xss_prof_reset": (None, []),
+    "xss_prof_read": (_I, [_I, ctypes.POINTER(ctypes.c_double),
+                           ctypes.POINTER(ctypes.c_ulonglong)]),
+    "xss_prof_launches": (ctypes.c_ulonglong, [_I]),
+    "xss_prof_kind_name": (ctypes.c_char_p, [_I]),
+}
+
+PROF_KINDS = ["hist", "onesweep", "fixup", "small_sort", "sel_hist", "sel_find",
+              "sel_collect", "sel_place", "seg_small", "seg_block", "seg_misc"]
+
+
+def prof_enable(on: bool) -> None:
+    lib().xss_prof_enable(int(on))
+
+
+def prof_reset() -> None:
+    lib().xss_prof_reset()
+
+
+def prof_read(kind: str):
+    """(total event-timed ms, timed launches) for a kernel kind since prof_reset()."""
+    ms = ctypes.c_double(0)
+    cnt = ctypes.c_ulonglong(0)
+    lib().xss_prof_read(PROF_KINDS.index(kind), ctypes.byref(ms), ctypes.byref(cnt))
+    return ms.value, cnt.value
+
+
+def prof_launches() -> int:
+    """Total kernel launches by the library so far (all kinds)."""
+    return sum(lib().xss_prof_launches(i) for i in range(len(PROF_KINDS)))
+
+
+def lib() -> ctypes.CDLL:
+    """Load libxss_gb300.so once; raise if it has not been built."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(f"{LIB_PATH} is missing: run __graft_entry__.build() first")
+        L = ctypes.CDLL(LIB_PATH)
+        for name, (res, args) in _SIGS.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+def dtype_id(dt) -> int:
+    name = np.dtype(dt).name if not isinstance(dt, str) else dt
+    if name not in DTYPES:
+        raise TypeError(f"unsupported key type {name}")
+    return DTYPES[name]
+
+
+def check(rc: int, what: str) -> None:
+    if rc != 0:
+        raise XssError(rc, what)
+
+
+def _ptr(a: np.ndarray) -> int:
+    if not a.flags.c_contiguous:
+        raise ValueError("array must be C-contiguous")
+    return a.ctypes.data
+
+
+# ---- host arrays (in place), reference names and defaults ---------------------
+def qsort(arr: np.ndarray, hasnan: bool = False, descending: bool = False) -> None:
+    check(lib().xss_qsort(dtype_id(arr.dtype), _ptr(arr), arr.size, int(hasnan),
+                          int(descending)), "qsort")
+
+
+def qselect(arr: np.ndarray, k: int, hasnan: bool = False, descending: bool = False) -> None:
+    check(lib().xss_qselect(dtype_id(arr.dtype), _ptr(arr), k, arr.size, int(hasnan),
+                            int(descending)), "qselect")
+
+
+def partial_qsort(arr: np.ndarray, k: int, hasnan: bool = False,
+                  descending: bool = False) -> None:
+    check(lib().xss_partial_qsort(dtype_id(arr.dtype), _ptr(arr), k, arr.size, int(hasnan),
+                                  int(descending)), "partial_qsort")
+
+
+def argsort(arr: np.ndarray, hasnan: bool = False, descending: bool = False) -> np.ndarray:
+    out = np.empty(arr.size, dtype=np.uint64)
+    check(lib().xss_argsort(dtype_id(arr.dtype), _ptr(arr), _ptr(out), arr.size, int(hasnan),
+                            int(descending)), "argsort")
+    return out
+
+
+def argselect(arr: np.ndarray, k: int, hasnan: bool = False) -> np.ndarray:
+    out = np.empty(arr.size, dtype=np.uint64)
+    check(lib().xss_argselect(dtype_id(arr.dtype), _ptr(arr), _ptr(out), k, arr.size,
+                              int(hasnan)), "argselect")
+    return out
+
+
+def keyvalue_qsort(keys: np.ndarray, vals: np.ndarray, hasnan: bool = False,
+                   descending: bool = False) -> None:
+    assert keys.size == vals.size
+    check(lib().xss_keyvalue_qsort(dtype_id(keys.dtype), dtype_id(vals.dtype), _ptr(keys),
+                                   _ptr(vals), keys.size, int(hasnan), int(descending)),
+          "keyvalue_qsort")
+
+
+def keyvalue_select(keys: np.ndarray, vals: np.ndarray, k: int, hasnan: bool = False,
+                    descending: bool = False) -> None:
+    assert keys.size == vals.size
+    check(lib().xss_keyvalue_select(dtype_id(keys.dtype), dtype_id(vals.dtype), _ptr(keys),
+                                    _ptr(vals), k, keys.size, int(hasnan), int(descending)),
+          "keyvalue_select")
+
+
+def keyvalue_partial_sort(keys: np.ndarray, vals: np.ndarray, k: int, hasnan: bool = False,
+                          descending: bool = False) -> None:
+    assert keys.size == vals.size
+    check(lib().xss_keyvalue_partial_sort(dtype_id(keys.dtype), dtype_id(vals.dtype),
+                                          _ptr(keys), _ptr(vals), k, keys.size, int(hasnan),
+                                          int(descending)), "keyvalue_partial_sort")
+
+
+# ---- device pointers ------------------------------------------------------------
+def workspace_size(op: str, key_dtype, n: int, k: int = 0, val_dtype="uint64") -> int:
+    return lib().xss_gpu_workspace_size(OPS[op], dtype_id(key_dtype), dtype_id(val_dtype), n, k)
+
+
+def stream_status(stream: int = 0) -> None:
+    check(lib().xss_gpu_stream_status(stream or None), "device status")
+
+
+def gpu_qsort(dt, d_arr: int, n: int, hasnan=False, descending=False, ws=0, ws_bytes=0,
+              stream=0) -> None:
+    check(lib().xss_gpu_qsort(dtype_id(dt), d_arr, n, int(hasnan), int(descending),
+                              ws or None, ws_bytes, stream or None), "gpu_qsort")
+
+
+def gpu_qselect(dt, d_arr, k, n, hasnan=False, descending=False, ws=0, ws_bytes=0, stream=0):
+    check(lib().xss_gpu_qselect(dtype_id(dt), d_arr, k, n, int(hasnan), int(descending),
+                                ws or None, ws_bytes, stream or None), "gpu_qselect")
+
+
+def gpu_partial_qsort(dt, d_arr, k, n, hasnan=False, descending=False, ws=0, ws_bytes=0,
+                      stream=0):
+    check(lib().xss_gpu_partial_qsort(dtype_id(dt), d_arr, k, n, int(hasnan), int(descending),
+                                      ws or None, ws_bytes, stream or None), "gpu_partial_qsort")
+
+
+def gpu_argsort(dt, d_arr, d_arg, n, hasnan=False, descending=False, ws=0, ws_bytes=0,
+                stream=0):
+    check(lib().xss_gpu_argsort(dtype_id(dt), d_arr, d_arg, n, int(hasnan), int(descending),
+                                ws or None, ws_bytes, stream or None), "gpu_argsort")
+
+
+def gpu_argselect(dt, d_arr, d_arg, k, n, hasnan=False, ws=0, ws_bytes=0, stream=0):
+    check(lib().xss_gpu_argselect(dtype_id(dt), d_arr, d_arg, k, n, int(hasnan), ws or None,
+                                  ws_bytes, stream or None), "gpu_argselect")
+
+
+def gpu_keyvalue_qsort(kdt, vdt, d_keys, d_vals, n, hasnan=False, descending=False, ws=0,
+                       ws_bytes=0, stream=0):
+    check(lib().xss_gpu_keyvalue_qsort(dtype_id(kdt), dtype_id(vdt), d_keys, d_vals, n,
+                                       int(hasnan), int(descending), ws or None, ws_bytes,
+                                       stream or None), "gpu_keyvalue_qsort")
+
+
+def gpu_keyvalue_select(kdt, vdt, d_keys, d_vals, k, n, hasnan=False, descending=False, ws=0,
+                        ws_bytes=0, stream=0):
+    check(lib().xss_gpu_keyvalue_select(dtype_id(kdt), dtype_id(vdt), d_keys, d_vals, k, n,
+                                        int(hasnan), int(descending), ws or None, ws_bytes,
+                                        stream or None), "gpu_keyvalue_select")
+
+
+def gpu_keyvalue_partial_sort(kdt, vdt, d_keys, d_vals, k, n, hasnan=False, descending=False,
+                              ws=0, ws_bytes=0, stream=0):
+    check(lib().xss_gpu_keyvalue_partial_sort(dtype_id(kdt), dtype_id(vdt), d_keys, d_vals, k,
+                                              n, int(hasnan), int(descending), ws or None,
+                                              ws_bytes, stream or None),
+          "gpu_keyvalue_partial_sort")
+
+
+def gpu_segmented_sort(kdt, vdt, d_keys, d_vals, d_offsets, h_offsets: np.ndarray,
+                       num_segments, hasnan=False, descending=False, ws=0, ws_bytes=0,
+                       stream=0):
+    hp = _ptr(h_offsets) if h_offsets is not None else None
+    check(lib().xss_gpu_segmented_sort(dtype_id(kdt), dtype_id(vdt) if vdt else -1, d_keys,
+                                       d_vals or None, d_offsets or None, hp, num_segments,
+                                       int(hasnan), int(descending), ws or None, ws_bytes,
+                                       stream or None), "gpu_segmented_sort")
+
+
+def segmented_workspace_size(kdt, vdt, h_offsets: np.ndarray) -> int:
+    return lib().xss_gpu_segmented_workspace_size(dtype_id(kdt), dtype_id(vdt) if vdt else -1,
+                                                  _ptr(h_offsets), h_offsets.size - 1)
