@@ -116,6 +116,28 @@ int xss_gpu_keyvalue_partial_sort(int key_dtype, int val_dtype, void *d_keys,
                                   xss_stream_t stream);
 
 /*
+ * Allocation-free device qsort.  No counterpart in the reference library.
+ *
+ * For callers that cannot allocate device memory when they sort: code running
+ * inside a memory allocator or an out-of-memory handler, plugins whose host
+ * application owns every device allocation, fixed-budget real-time loops.
+ * Same semantics as xss_gpu_qsort, but it never calls cudaMalloc / cudaFree or
+ * any allocating routine: its scratch is a fixed 12 MiB array compiled into
+ * the library's device image (held on every GPU that loads the library until
+ * the process exits), which limits n to XSS_NOALLOC_MAX_N keys of any type;
+ * larger n returns XSS_ETOOBIG without touching the array.
+ *
+ * The call is synchronous: it returns once the sort on `stream` is done, with
+ * XSS_OK or XSS_ETIMEOUT from the device-side checks.  The first call on each
+ * device looks up the array's device address; make that first call before any
+ * stream capture.  All calls share the one array: calls whose GPU work could
+ * overlap (other streams, other host threads) must be serialised by the caller.
+ */
+#define XSS_NOALLOC_MAX_N ((size_t)1 << 20)
+int xss_gpu_qsort_noalloc(int dtype, void *d_arr, size_t n, int hasnan, int descending,
+                          xss_stream_t stream);
+
+/*
  * Batched segmented sort: sorts each segment [offsets[i], offsets[i+1]) of
  * d_keys (and d_vals when non-NULL) independently, in one launch sequence.
  * d_offsets holds num_segments+1 non-decreasing uint64 offsets in device

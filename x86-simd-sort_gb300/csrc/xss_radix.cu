@@ -10,6 +10,7 @@
 // The reference's quicksort is in-place and unstable; an LSD radix sort is
 // stable per pass and yields one of the orders the reference may produce.
 #include <algorithm>
+#include <mutex>
 #include <type_traits>
 #include "xss_internal.cuh"
 
@@ -619,3 +620,139 @@ int radix_sort(int op, int kbytes, KeyXform xf, void *keys, void *vals, int vbyt
 }
 
 }  // namespace xss
+
+// ---------------------------------------------------------------------------
+// Allocation-free qsort: xss_gpu_qsort_noalloc.
+//
+// For callers that must not allocate device memory at call time -- code that
+// runs inside a memory allocator or an out-of-memory handler, plugins whose
+// host process owns every device allocation, fixed-budget real-time loops.
+// Its scratch is this file-scope device array instead of a cudaMalloc'd or
+// caller-provided workspace.  The array is part of the library's device image,
+// so every GPU that loads the library holds these bytes until the process
+// exits.  Every call uses the same array and finds the previous call's data
+// in it; the header and error word are cleared at the start of each call.
+// Calls whose work overlaps on the GPU (different streams, or different host
+// threads) race on the array and must be serialised by the caller.
+namespace xss {
+
+constexpr size_t NOALLOC_MAX_N = size_t(1) << 20;               // keys per call
+constexpr size_t NOALLOC_SCRATCH_BYTES = size_t(12) << 20;      // 12 MiB
+constexpr size_t NOALLOC_ERR_BYTES = 256;                       // error word slot
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_SCRATCH_BYTES];
+
+// Device address of g_noalloc_scratch, looked up once per device.  In host
+// code the symbol itself is only a host-side stand-in, never a device address.
+static std::mutex g_noalloc_mu;
+static unsigned char *g_noalloc_addr[64];
+
+static int noalloc_scratch(unsigned char **out)
+{
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return XSS_ECUDA;
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    if (!g_noalloc_addr[dev]) {
+        void *p = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess || p == nullptr) {
+            cudaGetLastError();
+            return XSS_ECUDA;
+        }
+        g_noalloc_addr[dev] = static_cast<unsigned char *>(p);
+    }
+    *out = g_noalloc_addr[dev];
+    return XSS_OK;
+}
+
+template <typename C>
+static int qsort_noalloc_c(KeyXform xf, void *keys, size_t n, unsigned char *scratch,
+                           cudaStream_t s)
+{
+    unsigned *err = reinterpret_cast<unsigned *>(scratch);
+    if (n <= SMALL_SORT_MAX) {
+        SmallArgs a{};
+        a.keys_in = keys;
+        a.keys_out = keys;
+        a.n = (uint32_t)n;
+        uint32_t npad = 2;
+        while (npad < n) npad <<= 1;
+        a.npad = npad;
+        a.xf = xf;
+        const size_t smem = align_up(sizeof(C) * npad, 16) + 2 * npad;  // <= 40 KiB
+        small_sort_kernel<C, NoVal><<<1, SMALL_BLOCK, smem, s>>>(a);
+        XSS_CUDA_TRY(cudaGetLastError());
+        return XSS_OK;
+    }
+    constexpr int BLOCK = TileCfg<C, NoVal>::BLOCK, ITEMS = TileCfg<C, NoVal>::ITEMS;
+    constexpr size_t TILE = (size_t)BLOCK * ITEMS;
+    const RadixLayout L = radix_layout(SOP_KEYS, sizeof(C), 0, n, TILE);
+    if (L.total > NOALLOC_SCRATCH_BYTES - NOALLOC_ERR_BYTES) return XSS_ENOMEM;
+    unsigned char *base = scratch + NOALLOC_ERR_BYTES;
+    RadixArgs a{};
+    a.kbuf[0] = keys;
+    a.kbuf[1] = base + L.k1;
+    a.kbuf[2] = base + L.k2;
+    a.n = n;
+    a.num_tiles = (uint32_t)((n + TILE - 1) / TILE);
+    a.passes = sizeof(C);
+    a.op = SOP_KEYS;
+    a.xf = xf;
+    a.hdr = reinterpret_cast<RadixHeader *>(base + L.hdr);
+    a.status = reinterpret_cast<uint32_t *>(base + L.status);
+    a.err = err;
+    XSS_CUDA_TRY(cudaMemsetAsync(a.hdr, 0, sizeof(RadixHeader), s));
+    const int sms = num_sms();
+    const size_t want = (n + 256 * 16 - 1) / (256 * 16);
+    const int hist_grid = (int)std::max<size_t>(1, std::min<size_t>(want, (size_t)sms * 8));
+    hist_kernel<C><<<hist_grid, 256, 0, s>>>(a);
+    XSS_CUDA_TRY(cudaGetLastError());
+    const size_t smem = TILE * sizeof(C);  // <= 24 KiB, no opt-in needed
+    for (int p = 0; p < a.passes; ++p) {
+        onesweep_kernel<C, NoVal, BLOCK, ITEMS><<<a.num_tiles, BLOCK, smem, s>>>(a, p);
+        XSS_CUDA_TRY(cudaGetLastError());
+    }
+    fixup_kernel<C, NoVal><<<sms * 2, 256, 0, s>>>(a);
+    XSS_CUDA_TRY(cudaGetLastError());
+    return XSS_OK;
+}
+
+}  // namespace xss
+
+extern "C" int xss_gpu_qsort_noalloc(int dtype, void *d_arr, size_t n, int hasnan,
+                                     int descending, xss_stream_t stream)
+{
+    using namespace xss;
+    int kbytes, kind;
+    switch (dtype) {
+    case XSS_DT_U16: kbytes = 2; kind = XK_UINT; break;
+    case XSS_DT_I16: kbytes = 2; kind = XK_INT; break;
+    case XSS_DT_F16: kbytes = 2; kind = XK_FLOAT; break;
+    case XSS_DT_U32: kbytes = 4; kind = XK_UINT; break;
+    case XSS_DT_I32: kbytes = 4; kind = XK_INT; break;
+    case XSS_DT_F32: kbytes = 4; kind = XK_FLOAT; break;
+    case XSS_DT_U64: kbytes = 8; kind = XK_UINT; break;
+    case XSS_DT_I64: kbytes = 8; kind = XK_INT; break;
+    case XSS_DT_F64: kbytes = 8; kind = XK_FLOAT; break;
+    default: return XSS_EINVAL;
+    }
+    if (n > NOALLOC_MAX_N) return XSS_ETOOBIG;
+    if (n > 1 && d_arr == nullptr) return XSS_EINVAL;
+    if (n <= 1) return XSS_OK;
+    cudaStream_t s = (cudaStream_t)stream;
+    unsigned char *scratch = nullptr;
+    int rc = noalloc_scratch(&scratch);
+    if (rc) return rc;
+    XSS_CUDA_TRY(cudaMemsetAsync(scratch, 0, NOALLOC_ERR_BYTES, s));
+    const KeyXform xf{kind, descending ? 1 : 0, hasnan ? 1 : 0};
+    switch (kbytes) {
+    case 2: rc = qsort_noalloc_c<uint16_t>(xf, d_arr, n, scratch, s); break;
+    case 4: rc = qsort_noalloc_c<uint32_t>(xf, d_arr, n, scratch, s); break;
+    default: rc = qsort_noalloc_c<uint64_t>(xf, d_arr, n, scratch, s); break;
+    }
+    if (rc) return rc;
+    unsigned h = 0;
+    XSS_CUDA_TRY(cudaMemcpyAsync(&h, scratch, sizeof(h), cudaMemcpyDeviceToHost, s));
+    XSS_CUDA_TRY(cudaStreamSynchronize(s));
+    return h ? XSS_ETIMEOUT : XSS_OK;
+}
