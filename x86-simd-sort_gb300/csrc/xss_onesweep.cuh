@@ -1,0 +1,470 @@
+// xss_onesweep.cuh -- the LSD radix pass ("onesweep": one read and one write
+// of keys and values per 8-bit digit, tile offsets by decoupled look-back).
+//
+// Two launch forms share the per-tile body `pass_tile`:
+//   onesweep_kernel          one CTA per tile, keys read with ordinary loads;
+//   onesweep_persist_kernel  resident CTAs that keep claiming tiles and
+//                            prefetch the next tile with a bulk copy (TMA).
+// Replaces the reference's vectorised partition sweeps
+// (src/xss-common-qsort.h:252-524, src/xss-common-keyvaluesort.hpp:109-379,
+// src/xss-common-argsort.h:174-422): each pass is a stable counting scatter
+// instead of an unstable in-place partition.
+#pragma once
+#include <type_traits>
+#include "xss_internal.cuh"
+#include "xss_tma.cuh"
+
+namespace xss {
+
+struct NoVal {};
+
+// Block-wide exclusive scan of one 32-bit value per thread.
+template <int BLOCK>
+__device__ __forceinline__ uint32_t block_excl_scan(uint32_t v, uint32_t *s_warp,
+                                                    uint32_t &total)
+{
+    constexpr int WARPS = BLOCK / 32;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) s_warp[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        uint32_t w = lane < WARPS ? s_warp[lane] : 0u;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            uint32_t y = __shfl_up_sync(0xffffffffu, w, o);
+            if (lane >= o) w += y;
+        }
+        if (lane < WARPS) s_warp[lane] = w;
+    }
+    __syncthreads();
+    const uint32_t pre = warp > 0 ? s_warp[warp - 1] : 0u;
+    total = s_warp[WARPS - 1];
+    __syncthreads();
+    return pre + x - v;
+}
+
+// Buffer id -> pointer without dynamically indexing the parameter array
+// (which would force a local-memory copy of it).
+__device__ __forceinline__ void *pick3(void *const (&b)[3], int i)
+{
+    return i == 0 ? b[0] : (i == 1 ? b[1] : b[2]);
+}
+
+// Tuning of one (key width, value width) instance.
+//   BLOCK, ITEMS: threads and keys per thread (tile = BLOCK * ITEMS)
+//   MINB:         CTAs per SM the register budget is cut for
+//   LB:           predecessors probed per look-back round trip
+//   RANK:         1 = peer masks from eight ballots, 0 = from shared atomicOr
+//   PERSIST:      1 = resident CTAs with TMA prefetch, 0 = one CTA per tile
+// Each line can be overridden at build time (a pre-included header defining
+// XSS_CFG_K32 etc.) for tuning.  Defaults are the fastest measured on GB300
+// (2^28 keys, uniform): keys-only 32-bit 4.95 ms/sort, int64->uint64 21.7 ms.
+template <int B, int I, int M, int L, int R, int P> struct CfgT {
+    static constexpr int BLOCK = B, ITEMS = I, MINB = M, LB = L, RANK = R, PERSIST = P;
+};
+#ifndef XSS_CFG_DEFAULT
+#define XSS_CFG_DEFAULT 256, 12, 2, 16, 1, 0
+#endif
+#ifndef XSS_CFG_K16
+#define XSS_CFG_K16 512, 16, 2, 16, 0, 1
+#endif
+#ifndef XSS_CFG_K32
+#define XSS_CFG_K32 512, 16, 2, 16, 0, 1
+#endif
+#ifndef XSS_CFG_K64
+#define XSS_CFG_K64 256, 16, 2, 16, 1, 1
+#endif
+#ifndef XSS_CFG_K32V32
+#define XSS_CFG_K32V32 512, 10, 2, 16, 1, 0
+#endif
+#ifndef XSS_CFG_K64V64
+#define XSS_CFG_K64V64 256, 12, 2, 16, 1, 0
+#endif
+template <typename C, typename V> struct PassCfg : CfgT<XSS_CFG_DEFAULT> {};
+template <> struct PassCfg<uint16_t, NoVal> : CfgT<XSS_CFG_K16> {};
+template <> struct PassCfg<uint32_t, NoVal> : CfgT<XSS_CFG_K32> {};
+template <> struct PassCfg<uint64_t, NoVal> : CfgT<XSS_CFG_K64> {};
+template <> struct PassCfg<uint32_t, uint32_t> : CfgT<XSS_CFG_K32V32> {};
+template <> struct PassCfg<uint64_t, uint64_t> : CfgT<XSS_CFG_K64V64> {};
+
+template <typename C, typename V> constexpr size_t pass_tile_size()
+{
+    return (size_t)PassCfg<C, V>::BLOCK * PassCfg<C, V>::ITEMS;
+}
+
+// Exclusive prefix of digit d over tiles [0, tile) by decoupled look-back:
+// probe LB predecessors per round trip, add aggregates until the first
+// inclusive prefix; an entry not yet published is probed again (bounded).
+#ifndef XSS_LOOKBACK_FIRST
+#define XSS_LOOKBACK_FIRST 16
+#endif
+template <int LB>
+__device__ __forceinline__ uint32_t lookback_excl(const uint32_t *st_pass, uint32_t tile, int d,
+                                                  unsigned *err)
+{
+    uint32_t excl = 0;
+    int p = (int)tile - 1;
+    uint32_t spins = 0;
+    // the first round probes only the nearest predecessors; later rounds LB
+    int width = XSS_LOOKBACK_FIRST < LB ? XSS_LOOKBACK_FIRST : LB;
+    while (p >= 0) {
+        uint32_t v[LB];
+#pragma unroll
+        for (int w = 0; w < LB; ++w)
+            v[w] = (w < width && p - w >= 0)
+                       ? ld_relaxed_u32(st_pass + (size_t)(p - w) * RADIX + d)
+                       : (p - w >= 0 ? 0u : FLAG_PRE);
+        int used = 0;
+        bool done = false;
+#pragma unroll
+        for (int w = 0; w < LB; ++w) {
+            if (done || used != w) break;
+            const uint32_t f = v[w] & FLAG_MASK;
+            if (f == 0u) break;
+            excl += v[w] & COUNT_MASK;
+            ++used;
+            if (f == FLAG_PRE) done = true;
+        }
+        if (done) return excl;
+        if (used == 0 && ++spins > XSS_SPIN_LIMIT) {
+            atomicOr(err, XSS_DEVERR_TIMEOUT);
+            return excl;
+        }
+        p -= used;
+        width = LB;
+    }
+    return excl;
+}
+
+// Shared-memory scratch of the per-tile body (static part).
+template <int BLOCK> struct PassSmem {
+    uint32_t whist[(BLOCK / 32) * RADIX];  // per-warp digit counts, then running offsets
+    uint32_t match[(BLOCK / 32) * RADIX];  // per-warp lane masks (kept zero between items)
+    int32_t off[RADIX];                     // global offset - local start, per digit
+    uint32_t scan[BLOCK / 32];
+};
+
+// Rank, publish, look up offsets and scatter one tile whose keys (codes) and
+// values are in registers.  s_k / s_v: TILE-sized staging buffers that no
+// thread reads any more once the first barrier here is passed.
+// after_rank() runs on every thread once the tile is staged (the persistent
+// form claims and prefetches its next tile there).
+// Pre: ps.whist is zero.  Post: zero again after the caller's next barrier.
+template <typename C, typename V, int BLOCK, int ITEMS, int LB, int RANK, typename VS,
+          typename AfterRank>
+__device__ __forceinline__ void pass_tile(const RadixArgs &a, const PassDesc &pd, int pass,
+                                          uint32_t tile, const C (&key)[ITEMS],
+                                          const VS (&val)[ITEMS], C *s_k, VS *s_v,
+                                          PassSmem<BLOCK> &ps, C *kdst, V *vdst,
+                                          AfterRank after_rank)
+{
+    constexpr int WARPS = BLOCK / 32;
+    constexpr int TILE = BLOCK * ITEMS;
+    constexpr bool HAS_V = !std::is_same<V, NoVal>::value;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const uint32_t n = (uint32_t)a.n;
+    const int shift = pass * RADIX_BITS;
+    const uint32_t tile_base = tile * (uint32_t)TILE;
+    uint32_t *wh = ps.whist + warp * RADIX;
+
+    // ---- per-warp digit counts (independent shared atomics)
+#pragma unroll
+    for (int j = 0; j < ITEMS; ++j) atomicAdd(&wh[uint32_t(key[j] >> shift) & (RADIX - 1)], 1u);
+    __syncthreads();
+
+    // ---- tile counts published at once, so successors' look-backs can pass
+    // this tile; then each warp's exclusive offset per digit
+    uint32_t *st_tile = a.status + ((size_t)pass * a.num_tiles + tile) * RADIX;
+    uint32_t cnt = 0;
+    if (tid < RADIX) {
+#pragma unroll
+        for (int w = 0; w < WARPS; ++w) cnt += ps.whist[w * RADIX + tid];
+        st_relaxed_u32(st_tile + tid, (tile == 0 ? FLAG_PRE : FLAG_AGG) | cnt);
+    }
+    uint32_t total;
+    const uint32_t local_start = block_excl_scan<BLOCK>(cnt, ps.scan, total);
+    if (tid < RADIX) {
+        uint32_t run = local_start;
+#pragma unroll
+        for (int w = 0; w < WARPS; ++w) {
+            const uint32_t c = ps.whist[w * RADIX + tid];
+            ps.whist[w * RADIX + tid] = run;
+            run += c;
+        }
+    }
+    __syncthreads();
+
+    // ---- stable rank (digit, warp, item, lane) and stage in digit order.
+    // The lanes sharing a digit find each other either by eight ballots, one
+    // per digit bit (RANK 1: no shared memory, consecutive items overlap), or
+    // through a per-warp word per digit that each lane sets its bit in and
+    // reads back (RANK 0: fewer instructions, the leader clears the word).
+    // The highest such lane advances the warp's running offset for the digit.
+    {
+        const uint32_t lt_mask = (1u << lane) - 1u;
+        uint32_t *mt = ps.match + warp * RADIX;
+#pragma unroll
+        for (int j = 0; j < ITEMS; ++j) {
+            const uint32_t d = uint32_t(key[j] >> shift) & (RADIX - 1);
+            uint32_t peers = 0xffffffffu;
+            if constexpr (RANK == 1) {
+#pragma unroll
+                for (int b = 0; b < RADIX_BITS; ++b) {
+                    const bool set = (d >> b) & 1u;
+                    const uint32_t m = __ballot_sync(0xffffffffu, set);
+                    peers &= set ? m : ~m;
+                }
+            } else {
+                atomicOr(&mt[d], 1u << lane);
+                __syncwarp();
+                peers = mt[d];
+                __syncwarp();
+            }
+            const int leader = 31 - __clz(peers);
+            uint32_t base = 0;
+            if (lane == leader) {
+                base = wh[d];
+                wh[d] = base + __popc(peers);
+                if constexpr (RANK == 0) mt[d] = 0;
+            }
+            base = __shfl_sync(0xffffffffu, base, leader);
+            const uint32_t p = base + __popc(peers & lt_mask);
+            s_k[p] = key[j];
+            if constexpr (HAS_V) s_v[p] = val[j];
+            __syncwarp();
+        }
+    }
+    after_rank();
+
+    // ---- look-back for this tile's global offsets
+    if (tid < RADIX) {
+        uint32_t excl = 0;
+        if (tile > 0) {
+            excl = lookback_excl<LB>(a.status + (size_t)pass * a.num_tiles * RADIX, tile, tid,
+                                     a.err);
+            st_relaxed_u32(st_tile + tid, FLAG_PRE | ((excl + cnt) & COUNT_MASK));
+        }
+        ps.off[tid] = (int32_t)(a.hdr->start[pass][tid] + excl) - (int32_t)local_start;
+    }
+    __syncthreads();
+
+    // ---- scatter runs of equal digits to consecutive global addresses
+    const uint32_t valid = min((uint32_t)TILE, n - tile_base);
+#pragma unroll
+    for (int m = 0; m < ITEMS; ++m) {
+        const uint32_t i = tid + m * BLOCK;
+        if (i < valid) {
+            const C c = s_k[i];
+            const uint32_t d = uint32_t(c >> shift) & (RADIX - 1);
+            const uint32_t g = (uint32_t)(ps.off[d] + (int32_t)i);
+            if (g < n) {
+                if (!pd.skip_keys) kdst[g] = pd.last ? from_code(c, a.xf) : c;
+                if constexpr (HAS_V) {
+                    if (pd.out_idx) a.out_idx[g] = (uint64_t)s_v[i];
+                    else vdst[g] = s_v[i];
+                }
+            } else {
+                atomicOr(a.err, XSS_DEVERR_BOUNDS);  // only after a look-back timeout
+            }
+        }
+    }
+    for (int i = tid; i < WARPS * RADIX; i += BLOCK) ps.whist[i] = 0;
+}
+
+struct NoAfterRank {
+    __device__ void operator()() const {}
+};
+
+// ---------------------------------------------------------------------------
+// One CTA per tile; the tile id comes from an in-order atomic counter, so a
+// tile only waits on tiles whose CTAs are already running.
+template <typename C, typename V, int BLOCK, int ITEMS, int MINB, int LB, int RANK>
+__global__ void __launch_bounds__(BLOCK, MINB) onesweep_kernel(RadixArgs a, int pass)
+{
+    constexpr int TILE = BLOCK * ITEMS;
+    constexpr bool HAS_V = !std::is_same<V, NoVal>::value;
+    using VS = typename std::conditional<HAS_V, V, uint8_t>::type;
+    static_assert(BLOCK >= RADIX, "one thread per digit");
+    const PassDesc pd = a.hdr->desc[pass];
+    if (!pd.active) return;
+
+    __shared__ PassSmem<BLOCK> ps;
+    __shared__ uint32_t s_tile;
+    extern __shared__ __align__(128) unsigned char s_dyn[];
+    C *s_k = reinterpret_cast<C *>(s_dyn);
+    VS *s_v = reinterpret_cast<VS *>(s_dyn + TILE * sizeof(C));
+
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    for (int i = tid; i < (BLOCK / 32) * RADIX; i += BLOCK) {
+        ps.whist[i] = 0;
+        ps.match[i] = 0;
+    }
+    if (tid == 0) s_tile = atomicAdd(&a.hdr->tile_ctr[pass], 1u);
+    __syncthreads();
+    const uint32_t tile = s_tile;
+    const uint32_t n = (uint32_t)a.n;
+    const uint32_t first_idx = tile * (uint32_t)TILE + (uint32_t)warp * (ITEMS * 32) + lane;
+    const C *ksrc = static_cast<const C *>(pick3(a.kbuf, pd.src));
+    C key[ITEMS];
+    VS val[ITEMS];
+#pragma unroll
+    for (int j = 0; j < ITEMS; ++j) {
+        const uint32_t idx = first_idx + j * 32;
+        if (idx < n) {
+            const C b = ksrc[idx];
+            key[j] = pd.first ? to_code(b, a.xf) : b;
+        } else {
+            key[j] = C(~C(0));
+        }
+    }
+    V *vdst = nullptr;
+    if constexpr (HAS_V) {
+        const V *vsrc = static_cast<const V *>(pick3(a.vbuf, pd.vsrc));
+        vdst = static_cast<V *>(pick3(a.vbuf, pd.vdst));
+#pragma unroll
+        for (int j = 0; j < ITEMS; ++j) {
+            const uint32_t idx = first_idx + j * 32;
+            val[j] = pd.gen_idx ? VS(idx) : (idx < n ? vsrc[idx] : VS(0));
+        }
+    }
+    pass_tile<C, V, BLOCK, ITEMS, LB, RANK>(a, pd, pass, tile, key, val, s_k, s_v, ps,
+                                      static_cast<C *>(pick3(a.kbuf, pd.dst)), vdst,
+                                      NoAfterRank{});
+}
+
+// ---------------------------------------------------------------------------
+// Resident CTAs that keep claiming tiles from the same in-order counter.
+// Once a tile is ranked and staged, the CTA claims its next tile and starts
+// its bulk copy (TMA) into the other buffer, so the load overlaps the current
+// tile's look-back and scatter.  Claims are in increasing order per CTA,
+// which keeps the look-back free of deadlock: the lowest unfinished tile is
+// always the current tile of the CTA holding it, and every tile below it is
+// finished.  Partial tiles and sources that are not 16-byte aligned are read
+// with ordinary loads.
+template <typename C, typename V, int BLOCK, int ITEMS, int MINB, int LB, int RANK>
+__global__ void __launch_bounds__(BLOCK, MINB) onesweep_persist_kernel(RadixArgs a, int pass)
+{
+    constexpr int TILE = BLOCK * ITEMS;
+    constexpr bool HAS_V = !std::is_same<V, NoVal>::value;
+    using VS = typename std::conditional<HAS_V, V, uint8_t>::type;
+    constexpr size_t VSZ = HAS_V ? sizeof(V) : 0;
+    static_assert(BLOCK >= RADIX, "one thread per digit");
+
+    const PassDesc pd = a.hdr->desc[pass];
+    if (!pd.active) return;
+
+    __shared__ PassSmem<BLOCK> ps;
+    __shared__ uint32_t s_tile[2];
+    __shared__ __align__(8) uint64_t s_bar[2];
+    extern __shared__ __align__(128) unsigned char s_dyn[];
+    C *const s_k0 = reinterpret_cast<C *>(s_dyn);
+    VS *const s_v0 = reinterpret_cast<VS *>(s_dyn + 2 * TILE * sizeof(C));
+
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const uint32_t n = (uint32_t)a.n;
+    const uint32_t num_tiles = a.num_tiles;
+    const C *ksrc = static_cast<const C *>(pick3(a.kbuf, pd.src));
+    C *kdst = static_cast<C *>(pick3(a.kbuf, pd.dst));
+    const V *vsrc = nullptr;
+    V *vdst = nullptr;
+    if constexpr (HAS_V) {
+        vsrc = static_cast<const V *>(pick3(a.vbuf, pd.vsrc));
+        vdst = static_cast<V *>(pick3(a.vbuf, pd.vdst));
+    }
+    const bool load_vals = HAS_V && !pd.gen_idx;
+    const bool tma = (reinterpret_cast<uintptr_t>(ksrc) & 15) == 0 &&
+                     (!load_vals || (reinterpret_cast<uintptr_t>(vsrc) & 15) == 0);
+    const uint32_t tile_bytes = TILE * (uint32_t)(sizeof(C) + (load_vals ? VSZ : 0));
+
+    auto issue = [&](uint32_t t, int b) {
+        const size_t base = (size_t)t * TILE;
+        mbar_arrive_expect_tx(&s_bar[b], tile_bytes);
+        bulk_load(s_k0 + b * TILE, ksrc + base, TILE * sizeof(C), &s_bar[b]);
+        if constexpr (HAS_V)
+            if (load_vals) bulk_load(s_v0 + b * TILE, vsrc + base, TILE * sizeof(VS), &s_bar[b]);
+    };
+    auto by_tma = [&](uint32_t t) { return tma && t < num_tiles && (size_t)t * TILE + TILE <= n; };
+
+    for (int i = tid; i < (BLOCK / 32) * RADIX; i += BLOCK) {
+        ps.whist[i] = 0;
+        ps.match[i] = 0;
+    }
+    if (tid == 0) {
+        mbar_init(&s_bar[0], 1);
+        mbar_init(&s_bar[1], 1);
+        fence_mbar_init();
+        const uint32_t t0 = atomicAdd(&a.hdr->tile_ctr[pass], 1u);
+        s_tile[0] = t0;
+        if (by_tma(t0)) issue(t0, 0);
+    }
+    __syncthreads();
+
+    uint32_t parity[2] = {0u, 0u};
+    for (uint32_t it = 0;; ++it) {
+        const int cur = it & 1;
+        const uint32_t tile = s_tile[cur];
+        if (tile >= num_tiles) break;
+        const uint32_t tile_base = tile * (uint32_t)TILE;
+        const uint32_t local0 = (uint32_t)warp * (ITEMS * 32) + lane;
+        C *s_k = s_k0 + cur * TILE;
+        VS *s_v = s_v0 + cur * TILE;
+        C key[ITEMS];
+        VS val[ITEMS];
+        if (by_tma(tile)) {
+            mbar_wait_bounded(&s_bar[cur], parity[cur], a.err);
+            parity[cur] ^= 1u;
+#pragma unroll
+            for (int j = 0; j < ITEMS; ++j) {
+                const C b = s_k[local0 + j * 32];
+                key[j] = pd.first ? to_code(b, a.xf) : b;
+            }
+            if constexpr (HAS_V) {
+#pragma unroll
+                for (int j = 0; j < ITEMS; ++j)
+                    val[j] = pd.gen_idx ? VS(tile_base + local0 + j * 32) : s_v[local0 + j * 32];
+            }
+        } else {
+#pragma unroll
+            for (int j = 0; j < ITEMS; ++j) {
+                const uint32_t idx = tile_base + local0 + j * 32;
+                if (idx < n) {
+                    const C b = ksrc[idx];
+                    key[j] = pd.first ? to_code(b, a.xf) : b;
+                } else {
+                    key[j] = C(~C(0));
+                }
+            }
+            if constexpr (HAS_V) {
+#pragma unroll
+                for (int j = 0; j < ITEMS; ++j) {
+                    const uint32_t idx = tile_base + local0 + j * 32;
+                    val[j] = pd.gen_idx ? VS(idx) : (idx < n ? vsrc[idx] : VS(0));
+                }
+            }
+        }
+        // pass_tile's first barrier orders these reads before the buffer is
+        // reused for staging; the other buffer was released by the previous
+        // iteration's final barrier, so the next tile may land there.
+        auto claim_next = [&]() {
+            if (tid == 0) {
+                const uint32_t t1 = atomicAdd(&a.hdr->tile_ctr[pass], 1u);
+                s_tile[cur ^ 1] = t1;
+                if (by_tma(t1)) {
+                    fence_proxy_async_smem();
+                    issue(t1, cur ^ 1);
+                }
+            }
+        };
+        pass_tile<C, V, BLOCK, ITEMS, LB, RANK>(a, pd, pass, tile, key, val, s_k, s_v, ps, kdst, vdst,
+                                          claim_next);
+        __syncthreads();
+    }
+}
+
+}  // namespace xss

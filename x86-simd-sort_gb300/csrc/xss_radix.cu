@@ -1,6 +1,6 @@
 // xss_radix.cu -- full sorts: one-CTA bitonic sort for small inputs and an
 // LSD "onesweep" radix sort (one up-front histogram, then one kernel per
-// 8-bit digit with a decoupled look-back prefix) for large ones.
+// 8-bit digit with a decoupled look-back prefix, xss_onesweep.cuh) for large ones.
 //
 // Replaces, for the reference's qsort / keyvalue_qsort / argsort:
 //   src/xss-common-qsort.h:529-605   (qsort_ recursion, partition sweeps)
@@ -10,45 +10,13 @@
 // The reference's quicksort is in-place and unstable; an LSD radix sort is
 // stable per pass and yields one of the orders the reference may produce.
 #include <algorithm>
+#include <cstdlib>
+#include <cstring>
 #include <mutex>
 #include <type_traits>
-#include "xss_internal.cuh"
+#include "xss_onesweep.cuh"
 
 namespace xss {
-
-struct NoVal {};
-
-// ---------------------------------------------------------------------------
-// Block-wide exclusive scan of one 32-bit value per thread.
-template <int BLOCK>
-__device__ __forceinline__ uint32_t block_excl_scan(uint32_t v, uint32_t *s_warp,
-                                                    uint32_t &total)
-{
-    constexpr int WARPS = BLOCK / 32;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    uint32_t x = v;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
-        if (lane >= o) x += y;
-    }
-    if (lane == 31) s_warp[warp] = x;
-    __syncthreads();
-    if (warp == 0) {
-        uint32_t w = lane < WARPS ? s_warp[lane] : 0u;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            uint32_t y = __shfl_up_sync(0xffffffffu, w, o);
-            if (lane >= o) w += y;
-        }
-        if (lane < WARPS) s_warp[lane] = w;
-    }
-    __syncthreads();
-    const uint32_t pre = warp > 0 ? s_warp[warp - 1] : 0u;
-    total = s_warp[WARPS - 1];
-    __syncthreads();
-    return pre + x - v;
-}
 
 // ---------------------------------------------------------------------------
 // Up-front histogram of every digit of every key (one read of the input),
@@ -154,193 +122,6 @@ __global__ void __launch_bounds__(256) hist_kernel(RadixArgs a)
     a.hdr->num_active = m;
 }
 
-// Buffer id -> pointer without dynamically indexing the parameter array
-// (which would force a local-memory copy of it).
-__device__ __forceinline__ void *pick3(void *const (&b)[3], int i)
-{
-    return i == 0 ? b[0] : (i == 1 ? b[1] : b[2]);
-}
-
-// ---------------------------------------------------------------------------
-// One LSD pass over 8 bits.  Each CTA takes the next tile id from an atomic
-// counter (so a tile only waits on tiles already running), ranks its keys by
-// digit with warp match + per-warp counters (stable: digit, warp, item, lane),
-// publishes its digit counts, resolves its global offsets by decoupled
-// look-back, stages the tile in digit order in shared memory and scatters
-// runs of equal digits to consecutive global addresses.
-template <typename C, typename V, int BLOCK, int ITEMS>
-__global__ void __launch_bounds__(BLOCK) onesweep_kernel(RadixArgs a, int pass)
-{
-    constexpr int WARPS = BLOCK / 32;
-    constexpr int TILE = BLOCK * ITEMS;
-    constexpr bool HAS_V = !std::is_same<V, NoVal>::value;
-    static_assert(BLOCK >= RADIX, "one thread per digit");
-
-    const PassDesc pd = a.hdr->desc[pass];
-    if (!pd.active) return;
-
-    __shared__ uint32_t s_whist[WARPS * RADIX];
-    __shared__ int32_t s_off[RADIX];
-    __shared__ uint32_t s_scan[WARPS];
-    __shared__ uint32_t s_tile;
-    extern __shared__ __align__(16) unsigned char s_stage[];
-
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const uint32_t n = (uint32_t)a.n;
-    const int shift = pass * RADIX_BITS;
-
-    for (int i = tid; i < WARPS * RADIX; i += BLOCK) s_whist[i] = 0;
-    if (tid == 0) s_tile = atomicAdd(&a.hdr->tile_ctr[pass], 1u);
-    __syncthreads();
-    const uint32_t tile = s_tile;
-    const uint32_t tile_base = tile * (uint32_t)TILE;
-    const uint32_t wbase = tile_base + (uint32_t)warp * (ITEMS * 32) + lane;
-
-    C key[ITEMS];
-    {
-        const C *ksrc = static_cast<const C *>(pick3(a.kbuf, pd.src));
-#pragma unroll
-        for (int j = 0; j < ITEMS; ++j) {
-            const uint32_t idx = wbase + j * 32;
-            if (idx < n) {
-                const C b = ksrc[idx];
-                key[j] = pd.first ? to_code(b, a.xf) : b;
-            } else {
-                key[j] = C(~C(0));
-            }
-        }
-    }
-    typename std::conditional<HAS_V, V, uint8_t>::type val[ITEMS];
-    if constexpr (HAS_V) {
-        const V *vsrc = static_cast<const V *>(pick3(a.vbuf, pd.vsrc));
-#pragma unroll
-        for (int j = 0; j < ITEMS; ++j) {
-            const uint32_t idx = wbase + j * 32;
-            if (pd.gen_idx) val[j] = V(idx);
-            else val[j] = idx < n ? vsrc[idx] : V(0);
-        }
-    }
-
-    // ---- stable rank within the tile
-    uint32_t pos[ITEMS];
-    {
-        uint32_t *wh = s_whist + warp * RADIX;
-        const uint32_t lt_mask = (1u << lane) - 1u;
-#pragma unroll
-        for (int j = 0; j < ITEMS; ++j) {
-            const uint32_t d = uint32_t(key[j] >> shift) & (RADIX - 1);
-            const uint32_t peers = __match_any_sync(0xffffffffu, d);
-            const int leader = 31 - __clz(peers);
-            uint32_t base = 0;
-            if (lane == leader) {
-                base = wh[d];
-                wh[d] = base + __popc(peers);
-            }
-            base = __shfl_sync(0xffffffffu, base, leader);
-            pos[j] = base + __popc(peers & lt_mask);
-            __syncwarp();
-        }
-    }
-    __syncthreads();
-
-    // ---- tile digit counts, publish, local scan, look-back
-    uint32_t cnt = 0;
-    uint32_t *st_tile = a.status + ((size_t)pass * a.num_tiles + tile) * RADIX;
-    if (tid < RADIX) {
-        uint32_t run = 0;
-#pragma unroll
-        for (int w = 0; w < WARPS; ++w) {
-            const uint32_t c = s_whist[w * RADIX + tid];
-            s_whist[w * RADIX + tid] = run;
-            run += c;
-        }
-        cnt = run;
-        st_relaxed_u32(st_tile + tid, (tile == 0 ? FLAG_PRE : FLAG_AGG) | cnt);
-    }
-    uint32_t total;
-    const uint32_t local_start = block_excl_scan<BLOCK>(cnt, s_scan, total);
-    if (tid < RADIX) {
-        uint32_t excl = 0;
-        if (tile > 0) {
-            const uint32_t *st_pass = a.status + (size_t)pass * a.num_tiles * RADIX;
-            int p = (int)tile - 1;
-            uint32_t spins = 0;
-            while (p >= 0) {
-                const uint32_t v = ld_relaxed_u32(st_pass + (size_t)p * RADIX + tid);
-                const uint32_t f = v & FLAG_MASK;
-                if (f == 0u) {
-                    if (++spins > XSS_SPIN_LIMIT) {
-                        atomicOr(a.err, XSS_DEVERR_TIMEOUT);
-                        break;
-                    }
-                    continue;
-                }
-                excl += v & COUNT_MASK;
-                if (f == FLAG_PRE) break;
-                --p;
-            }
-            st_relaxed_u32(st_tile + tid, FLAG_PRE | ((excl + cnt) & COUNT_MASK));
-        }
-        s_off[tid] = (int32_t)(a.hdr->start[pass][tid] + excl) - (int32_t)local_start;
-#pragma unroll
-        for (int w = 0; w < WARPS; ++w) s_whist[w * RADIX + tid] += local_start;
-    }
-    __syncthreads();
-
-    // ---- stage keys in digit order
-    C *s_keys = reinterpret_cast<C *>(s_stage);
-#pragma unroll
-    for (int j = 0; j < ITEMS; ++j) {
-        const uint32_t d = uint32_t(key[j] >> shift) & (RADIX - 1);
-        pos[j] += s_whist[warp * RADIX + d];
-        s_keys[pos[j]] = key[j];
-    }
-    __syncthreads();
-
-    // ---- scatter: consecutive threads write consecutive slots of a digit run
-    const uint32_t valid = min((uint32_t)TILE, n - tile_base);
-    uint32_t gdst[HAS_V ? ITEMS : 1];
-    {
-        C *kdst = static_cast<C *>(pick3(a.kbuf, pd.dst));
-#pragma unroll
-        for (int m = 0; m < ITEMS; ++m) {
-            const uint32_t i = tid + m * BLOCK;
-            if (i < valid) {
-                const C c = s_keys[i];
-                const uint32_t d = uint32_t(c >> shift) & (RADIX - 1);
-                uint32_t g = (uint32_t)(s_off[d] + (int32_t)i);
-                if (g >= n) {  // only reachable after a look-back timeout
-                    atomicOr(a.err, XSS_DEVERR_BOUNDS);
-                    g = n;     // marks the slot as not to be written
-                }
-                if constexpr (HAS_V) gdst[m] = g;
-                if (!pd.skip_keys && g < n) kdst[g] = pd.last ? from_code(c, a.xf) : c;
-            }
-        }
-    }
-    if constexpr (HAS_V) {
-        __syncthreads();
-        V *s_vals = reinterpret_cast<V *>(s_stage);
-#pragma unroll
-        for (int j = 0; j < ITEMS; ++j) s_vals[pos[j]] = val[j];
-        __syncthreads();
-        if (pd.out_idx) {
-#pragma unroll
-            for (int m = 0; m < ITEMS; ++m) {
-                const uint32_t i = tid + m * BLOCK;
-                if (i < valid && gdst[m] < n) a.out_idx[gdst[m]] = (uint64_t)s_vals[i];
-            }
-        } else {
-            V *vdst = static_cast<V *>(pick3(a.vbuf, pd.vdst));
-#pragma unroll
-            for (int m = 0; m < ITEMS; ++m) {
-                const uint32_t i = tid + m * BLOCK;
-                if (i < valid && gdst[m] < n) vdst[gdst[m]] = s_vals[i];
-            }
-        }
-    }
-}
-
 // ---------------------------------------------------------------------------
 // Finishing step after the passes: copy back when an odd number of passes
 // ran, canonicalise NaNs when no pass ran, or write the identity permutation.
@@ -423,7 +204,7 @@ __global__ void __launch_bounds__(SMALL_BLOCK) small_sort_kernel(SmallArgs a)
         for (uint32_t i = tid; i < n; i += SMALL_BLOCK) a.out_idx[i] = s_idx[i];
     }
     if constexpr (HAS_V) {
-        constexpr int R = (int)(SMALL_SORT_MAX * 2 / SMALL_BLOCK);
+        constexpr int R = (int)(SMALL_SORT_MAX / SMALL_BLOCK);
         const V *vin = static_cast<const V *>(a.vals_in);
         V tmp[R];
 #pragma unroll
@@ -443,20 +224,6 @@ __global__ void __launch_bounds__(SMALL_BLOCK) small_sort_kernel(SmallArgs a)
 
 // ---------------------------------------------------------------------------
 // Host side.
-template <typename C, typename V> struct TileCfg {
-    static constexpr int BLOCK = 256;
-    static constexpr int ITEMS = (sizeof(C) + sizeof(V) > 8) ? 8 : 16;
-};
-template <typename C> struct TileCfg<C, NoVal> {
-    static constexpr int BLOCK = 256;
-    static constexpr int ITEMS = sizeof(C) == 8 ? 12 : 16;
-};
-
-template <typename C, typename V> constexpr size_t tile_size()
-{
-    return (size_t)TileCfg<C, V>::BLOCK * TileCfg<C, V>::ITEMS;
-}
-
 struct RadixLayout {
     size_t hdr, status, k1, k2, v1, v2, total;
 };
@@ -478,18 +245,13 @@ static RadixLayout radix_layout(int op, int kbytes, int vbytes, size_t n, size_t
     return L;
 }
 
-template <typename C, typename V> static size_t tile_for()
-{
-    return tile_size<C, V>();
-}
-
 static size_t tile_for_bytes(int op, int kbytes, int vbytes)
 {
     const int vb = (op == SOP_ARG) ? 4 : (op == SOP_KV ? vbytes : 0);
     switch (kbytes) {
-    case 2: return vb == 0 ? tile_for<uint16_t, NoVal>() : vb == 4 ? tile_for<uint16_t, uint32_t>() : tile_for<uint16_t, uint64_t>();
-    case 4: return vb == 0 ? tile_for<uint32_t, NoVal>() : vb == 4 ? tile_for<uint32_t, uint32_t>() : tile_for<uint32_t, uint64_t>();
-    default: return vb == 0 ? tile_for<uint64_t, NoVal>() : vb == 4 ? tile_for<uint64_t, uint32_t>() : tile_for<uint64_t, uint64_t>();
+    case 2: return vb == 0 ? pass_tile_size<uint16_t, NoVal>() : vb == 4 ? pass_tile_size<uint16_t, uint32_t>() : pass_tile_size<uint16_t, uint64_t>();
+    case 4: return vb == 0 ? pass_tile_size<uint32_t, NoVal>() : vb == 4 ? pass_tile_size<uint32_t, uint32_t>() : pass_tile_size<uint32_t, uint64_t>();
+    default: return vb == 0 ? pass_tile_size<uint64_t, NoVal>() : vb == 4 ? pass_tile_size<uint64_t, uint32_t>() : pass_tile_size<uint64_t, uint64_t>();
     }
 }
 
@@ -499,9 +261,25 @@ size_t radix_workspace_bytes(int op, int kbytes, int vbytes, size_t n)
     return radix_layout(op, kbytes, vbytes, n, tile_for_bytes(op, kbytes, vbytes)).total;
 }
 
+// How a sort is launched: where device-side errors go and whether launches
+// go through the profiler hooks (which may create CUDA events).
+struct LaunchOpts {
+    unsigned *err;
+    bool instrument;
+};
+
+#define XSS_LAUNCH_OPT(opts, kind, stream, ...) \
+    do {                                        \
+        if ((opts).instrument) {                \
+            XSS_LAUNCH(kind, stream, __VA_ARGS__); \
+        } else {                                \
+            __VA_ARGS__;                        \
+        }                                       \
+    } while (0)
+
 template <typename C, typename V>
 static int small_sort_launch(int op, KeyXform xf, void *keys, void *vals,
-                             uint64_t *out_idx, size_t n, cudaStream_t s)
+                             uint64_t *out_idx, size_t n, cudaStream_t s, const LaunchOpts &o)
 {
     SmallArgs a{};
     a.keys_in = keys;
@@ -514,28 +292,38 @@ static int small_sort_launch(int op, KeyXform xf, void *keys, void *vals,
     while (npad < n) npad <<= 1;
     a.npad = npad;
     a.xf = xf;
-    const size_t smem = align_up(sizeof(C) * npad, 16) + 2 * npad;
-    auto kern = small_sort_kernel<C, V>;
-    static bool attr_set = false;
-    if (!attr_set) {
-        XSS_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                          (int)(align_up(sizeof(C) * SMALL_SORT_MAX * 2, 16) + 4 * SMALL_SORT_MAX)));
-        attr_set = true;
-    }
-    XSS_LAUNCH(PK_SMALL, s, kern<<<1, SMALL_BLOCK, smem, s>>>(a));
+    const size_t smem = align_up(sizeof(C) * npad, 16) + 2 * npad;  // <= 40 KiB
+    XSS_LAUNCH_OPT(o, PK_SMALL, s, small_sort_kernel<C, V><<<1, SMALL_BLOCK, smem, s>>>(a));
     XSS_CUDA_TRY(cudaGetLastError());
     return XSS_OK;
 }
 
-template <typename C, typename V>
-static int onesweep_launch(int op, KeyXform xf, void *keys, void *vals,
-                           uint64_t *out_idx, size_t n, void *ws, size_t ws_bytes,
-                           cudaStream_t s)
+// Pass-kernel form: the tuned choice of PassCfg (PERSIST), unless the
+// environment forces one: XSS_ONESWEEP=tile (one CTA per tile) or
+// XSS_ONESWEEP=persist (resident CTAs with TMA prefetch).
+static bool use_persistent_pass(bool tuned)
 {
-    constexpr int BLOCK = TileCfg<C, V>::BLOCK, ITEMS = TileCfg<C, V>::ITEMS;
+    static const int forced = [] {
+        const char *e = getenv("XSS_ONESWEEP");
+        if (e && strcmp(e, "tile") == 0) return 0;
+        if (e && strcmp(e, "persist") == 0) return 1;
+        return -1;
+    }();
+    return forced < 0 ? tuned : forced == 1;
+}
+
+template <typename C, typename V>
+static int onesweep_launch(int op, KeyXform xf, void *keys, void *vals, uint64_t *out_idx,
+                           size_t n, void *ws, size_t ws_bytes, cudaStream_t s,
+                           const LaunchOpts &o)
+{
+    using Cfg = PassCfg<C, V>;
+    constexpr int BLOCK = Cfg::BLOCK, ITEMS = Cfg::ITEMS, MINB = Cfg::MINB, LB = Cfg::LB,
+                  RANK = Cfg::RANK;
     constexpr size_t TILE = (size_t)BLOCK * ITEMS;
+    constexpr bool HAS_V = !std::is_same<V, NoVal>::value;
     const int kbytes = sizeof(C);
-    const int vbytes = std::is_same<V, NoVal>::value ? 0 : (int)sizeof(V);
+    const int vbytes = HAS_V ? (int)sizeof(V) : 0;
     const RadixLayout L = radix_layout(op, kbytes, op == SOP_ARG ? 4 : vbytes, n, TILE);
     if (ws == nullptr || ws_bytes < L.total) return XSS_ENOMEM;
     char *base = static_cast<char *>(ws);
@@ -555,53 +343,80 @@ static int onesweep_launch(int op, KeyXform xf, void *keys, void *vals,
     a.xf = xf;
     a.hdr = reinterpret_cast<RadixHeader *>(base + L.hdr);
     a.status = reinterpret_cast<uint32_t *>(base + L.status);
-    a.err = device_error_word();
+    a.err = o.err;
+    if (!a.err) return XSS_ECUDA;
 
     XSS_CUDA_TRY(cudaMemsetAsync(a.hdr, 0, sizeof(RadixHeader), s));
     const int sms = num_sms();
     const size_t want = (n + 256 * 16 - 1) / (256 * 16);
     const int hist_grid = (int)std::max<size_t>(1, std::min<size_t>(want, (size_t)sms * 8));
-    XSS_LAUNCH(PK_HIST, s, hist_kernel<C><<<hist_grid, 256, 0, s>>>(a));
+    XSS_LAUNCH_OPT(o, PK_HIST, s, hist_kernel<C><<<hist_grid, 256, 0, s>>>(a));
     XSS_CUDA_TRY(cudaGetLastError());
 
-    const size_t smem = TILE * std::max(sizeof(C), std::is_same<V, NoVal>::value ? (size_t)0 : sizeof(V));
-    auto kern = onesweep_kernel<C, V, BLOCK, ITEMS>;
-    static bool attr_set = false;
-    if (!attr_set) {
-        XSS_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        attr_set = true;
+    const size_t vsz = HAS_V ? sizeof(V) : 0;
+    if (use_persistent_pass(Cfg::PERSIST != 0)) {
+        const size_t smem = 2 * TILE * (sizeof(C) + vsz);
+        auto kern = onesweep_persist_kernel<C, V, BLOCK, ITEMS, MINB, LB, RANK>;
+        static int per_sm = 0;
+        if (!per_sm) {
+            XSS_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                              (int)smem));
+            int v = 0;
+            XSS_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, kern, BLOCK, smem));
+            per_sm = std::max(v, 1);
+        }
+        const uint32_t grid = (uint32_t)std::min<size_t>(a.num_tiles, (size_t)per_sm * sms);
+        for (int p = 0; p < a.passes; ++p) {
+            XSS_LAUNCH_OPT(o, PK_ONESWEEP, s, kern<<<grid, BLOCK, smem, s>>>(a, p));
+            XSS_CUDA_TRY(cudaGetLastError());
+        }
+    } else {
+        const size_t smem = TILE * (sizeof(C) + vsz);
+        auto kern = onesweep_kernel<C, V, BLOCK, ITEMS, MINB, LB, RANK>;
+        static bool attr_set = false;
+        if (!attr_set) {
+            XSS_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                              (int)smem));
+            attr_set = true;
+        }
+        for (int p = 0; p < a.passes; ++p) {
+            XSS_LAUNCH_OPT(o, PK_ONESWEEP, s, kern<<<a.num_tiles, BLOCK, smem, s>>>(a, p));
+            XSS_CUDA_TRY(cudaGetLastError());
+        }
     }
-    for (int p = 0; p < a.passes; ++p) {
-        XSS_LAUNCH(PK_ONESWEEP, s, kern<<<a.num_tiles, BLOCK, smem, s>>>(a, p));
-        XSS_CUDA_TRY(cudaGetLastError());
-    }
-    XSS_LAUNCH(PK_FIXUP, s, fixup_kernel<C, V><<<sms * 2, 256, 0, s>>>(a));
+    XSS_LAUNCH_OPT(o, PK_FIXUP, s, fixup_kernel<C, V><<<sms * 2, 256, 0, s>>>(a));
     XSS_CUDA_TRY(cudaGetLastError());
     return XSS_OK;
 }
 
 template <typename C>
 static int radix_sort_c(int op, KeyXform xf, void *keys, void *vals, int vbytes,
-                        uint64_t *out_idx, size_t n, void *ws, size_t ws_bytes, cudaStream_t s)
+                        uint64_t *out_idx, size_t n, void *ws, size_t ws_bytes, cudaStream_t s,
+                        const LaunchOpts &o)
 {
     const bool small = n <= SMALL_SORT_MAX;
     if (op == SOP_ARG) {
-        return small ? small_sort_launch<C, NoVal>(op, xf, keys, nullptr, out_idx, n, s)
-                     : onesweep_launch<C, uint32_t>(op, xf, keys, nullptr, out_idx, n, ws, ws_bytes, s);
+        return small ? small_sort_launch<C, NoVal>(op, xf, keys, nullptr, out_idx, n, s, o)
+                     : onesweep_launch<C, uint32_t>(op, xf, keys, nullptr, out_idx, n, ws,
+                                                    ws_bytes, s, o);
     }
     if (op == SOP_KEYS || vbytes == 0) {
-        return small ? small_sort_launch<C, NoVal>(op, xf, keys, nullptr, nullptr, n, s)
-                     : onesweep_launch<C, NoVal>(op, xf, keys, nullptr, nullptr, n, ws, ws_bytes, s);
+        return small ? small_sort_launch<C, NoVal>(op, xf, keys, nullptr, nullptr, n, s, o)
+                     : onesweep_launch<C, NoVal>(op, xf, keys, nullptr, nullptr, n, ws, ws_bytes,
+                                                 s, o);
     }
     if (vbytes == 4)
-        return small ? small_sort_launch<C, uint32_t>(op, xf, keys, vals, nullptr, n, s)
-                     : onesweep_launch<C, uint32_t>(op, xf, keys, vals, nullptr, n, ws, ws_bytes, s);
-    return small ? small_sort_launch<C, uint64_t>(op, xf, keys, vals, nullptr, n, s)
-                 : onesweep_launch<C, uint64_t>(op, xf, keys, vals, nullptr, n, ws, ws_bytes, s);
+        return small ? small_sort_launch<C, uint32_t>(op, xf, keys, vals, nullptr, n, s, o)
+                     : onesweep_launch<C, uint32_t>(op, xf, keys, vals, nullptr, n, ws, ws_bytes,
+                                                    s, o);
+    return small ? small_sort_launch<C, uint64_t>(op, xf, keys, vals, nullptr, n, s, o)
+                 : onesweep_launch<C, uint64_t>(op, xf, keys, vals, nullptr, n, ws, ws_bytes, s,
+                                                o);
 }
 
-int radix_sort(int op, int kbytes, KeyXform xf, void *keys, void *vals, int vbytes,
-               uint64_t *out_idx, size_t n, void *ws, size_t ws_bytes, cudaStream_t s)
+static int radix_sort_opts(int op, int kbytes, KeyXform xf, void *keys, void *vals, int vbytes,
+                           uint64_t *out_idx, size_t n, void *ws, size_t ws_bytes,
+                           cudaStream_t s, const LaunchOpts &o)
 {
     if (n == 0) return XSS_OK;
     if (n == 1) {
@@ -612,11 +427,21 @@ int radix_sort(int op, int kbytes, KeyXform xf, void *keys, void *vals, int vbyt
     }
     if (n > XSS_MAX_N) return XSS_ETOOBIG;
     switch (kbytes) {
-    case 2: return radix_sort_c<uint16_t>(op, xf, keys, vals, vbytes, out_idx, n, ws, ws_bytes, s);
-    case 4: return radix_sort_c<uint32_t>(op, xf, keys, vals, vbytes, out_idx, n, ws, ws_bytes, s);
-    case 8: return radix_sort_c<uint64_t>(op, xf, keys, vals, vbytes, out_idx, n, ws, ws_bytes, s);
+    case 2: return radix_sort_c<uint16_t>(op, xf, keys, vals, vbytes, out_idx, n, ws, ws_bytes, s, o);
+    case 4: return radix_sort_c<uint32_t>(op, xf, keys, vals, vbytes, out_idx, n, ws, ws_bytes, s, o);
+    case 8: return radix_sort_c<uint64_t>(op, xf, keys, vals, vbytes, out_idx, n, ws, ws_bytes, s, o);
     default: return XSS_EINVAL;
     }
+}
+
+int radix_sort(int op, int kbytes, KeyXform xf, void *keys, void *vals, int vbytes,
+               uint64_t *out_idx, size_t n, void *ws, size_t ws_bytes, cudaStream_t s)
+{
+    if (n <= 1 || n > XSS_MAX_N)
+        return radix_sort_opts(op, kbytes, xf, keys, vals, vbytes, out_idx, n, ws, ws_bytes, s,
+                               LaunchOpts{nullptr, true});
+    const LaunchOpts o{device_error_word(), true};
+    return radix_sort_opts(op, kbytes, xf, keys, vals, vbytes, out_idx, n, ws, ws_bytes, s, o);
 }
 
 }  // namespace xss
@@ -665,58 +490,6 @@ static int noalloc_scratch(unsigned char **out)
     return XSS_OK;
 }
 
-template <typename C>
-static int qsort_noalloc_c(KeyXform xf, void *keys, size_t n, unsigned char *scratch,
-                           cudaStream_t s)
-{
-    unsigned *err = reinterpret_cast<unsigned *>(scratch);
-    if (n <= SMALL_SORT_MAX) {
-        SmallArgs a{};
-        a.keys_in = keys;
-        a.keys_out = keys;
-        a.n = (uint32_t)n;
-        uint32_t npad = 2;
-        while (npad < n) npad <<= 1;
-        a.npad = npad;
-        a.xf = xf;
-        const size_t smem = align_up(sizeof(C) * npad, 16) + 2 * npad;  // <= 40 KiB
-        small_sort_kernel<C, NoVal><<<1, SMALL_BLOCK, smem, s>>>(a);
-        XSS_CUDA_TRY(cudaGetLastError());
-        return XSS_OK;
-    }
-    constexpr int BLOCK = TileCfg<C, NoVal>::BLOCK, ITEMS = TileCfg<C, NoVal>::ITEMS;
-    constexpr size_t TILE = (size_t)BLOCK * ITEMS;
-    const RadixLayout L = radix_layout(SOP_KEYS, sizeof(C), 0, n, TILE);
-    if (L.total > NOALLOC_SCRATCH_BYTES - NOALLOC_ERR_BYTES) return XSS_ENOMEM;
-    unsigned char *base = scratch + NOALLOC_ERR_BYTES;
-    RadixArgs a{};
-    a.kbuf[0] = keys;
-    a.kbuf[1] = base + L.k1;
-    a.kbuf[2] = base + L.k2;
-    a.n = n;
-    a.num_tiles = (uint32_t)((n + TILE - 1) / TILE);
-    a.passes = sizeof(C);
-    a.op = SOP_KEYS;
-    a.xf = xf;
-    a.hdr = reinterpret_cast<RadixHeader *>(base + L.hdr);
-    a.status = reinterpret_cast<uint32_t *>(base + L.status);
-    a.err = err;
-    XSS_CUDA_TRY(cudaMemsetAsync(a.hdr, 0, sizeof(RadixHeader), s));
-    const int sms = num_sms();
-    const size_t want = (n + 256 * 16 - 1) / (256 * 16);
-    const int hist_grid = (int)std::max<size_t>(1, std::min<size_t>(want, (size_t)sms * 8));
-    hist_kernel<C><<<hist_grid, 256, 0, s>>>(a);
-    XSS_CUDA_TRY(cudaGetLastError());
-    const size_t smem = TILE * sizeof(C);  // <= 24 KiB, no opt-in needed
-    for (int p = 0; p < a.passes; ++p) {
-        onesweep_kernel<C, NoVal, BLOCK, ITEMS><<<a.num_tiles, BLOCK, smem, s>>>(a, p);
-        XSS_CUDA_TRY(cudaGetLastError());
-    }
-    fixup_kernel<C, NoVal><<<sms * 2, 256, 0, s>>>(a);
-    XSS_CUDA_TRY(cudaGetLastError());
-    return XSS_OK;
-}
-
 }  // namespace xss
 
 extern "C" int xss_gpu_qsort_noalloc(int dtype, void *d_arr, size_t n, int hasnan,
@@ -739,17 +512,20 @@ extern "C" int xss_gpu_qsort_noalloc(int dtype, void *d_arr, size_t n, int hasna
     if (n > NOALLOC_MAX_N) return XSS_ETOOBIG;
     if (n > 1 && d_arr == nullptr) return XSS_EINVAL;
     if (n <= 1) return XSS_OK;
+    // the scratch layout for the largest call must fit the array
+    if (radix_workspace_bytes(SOP_KEYS, kbytes, 0, NOALLOC_MAX_N) >
+        NOALLOC_SCRATCH_BYTES - NOALLOC_ERR_BYTES)
+        return XSS_ENOMEM;
     cudaStream_t s = (cudaStream_t)stream;
     unsigned char *scratch = nullptr;
     int rc = noalloc_scratch(&scratch);
     if (rc) return rc;
     XSS_CUDA_TRY(cudaMemsetAsync(scratch, 0, NOALLOC_ERR_BYTES, s));
     const KeyXform xf{kind, descending ? 1 : 0, hasnan ? 1 : 0};
-    switch (kbytes) {
-    case 2: rc = qsort_noalloc_c<uint16_t>(xf, d_arr, n, scratch, s); break;
-    case 4: rc = qsort_noalloc_c<uint32_t>(xf, d_arr, n, scratch, s); break;
-    default: rc = qsort_noalloc_c<uint64_t>(xf, d_arr, n, scratch, s); break;
-    }
+    const LaunchOpts o{reinterpret_cast<unsigned *>(scratch), false};
+    rc = radix_sort_opts(SOP_KEYS, kbytes, xf, d_arr, nullptr, 0, nullptr, n,
+                         scratch + NOALLOC_ERR_BYTES, NOALLOC_SCRATCH_BYTES - NOALLOC_ERR_BYTES,
+                         s, o);
     if (rc) return rc;
     unsigned h = 0;
     XSS_CUDA_TRY(cudaMemcpyAsync(&h, scratch, sizeof(h), cudaMemcpyDeviceToHost, s));

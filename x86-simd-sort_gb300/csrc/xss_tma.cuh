@@ -1,0 +1,77 @@
+// xss_tma.cuh -- 1-D bulk copies (TMA, cp.async.bulk) into shared memory
+// completed through an mbarrier, and the bounded wait on that barrier.
+#pragma once
+#include <cstdint>
+#include "xss_keys.cuh"
+
+namespace xss {
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p)
+{
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count)
+                 : "memory");
+}
+
+// Make barrier initialisation visible to the async (TMA) proxy.
+__device__ __forceinline__ void fence_mbar_init()
+{
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+// Order this thread's earlier generic-proxy shared-memory accesses (made
+// visible to it by a preceding __syncthreads) before later async-proxy writes.
+__device__ __forceinline__ void fence_proxy_async_smem()
+{
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *bar, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+                 "r"(bytes)
+                 : "memory");
+}
+
+// Copy `bytes` (multiple of 16; both addresses 16-byte aligned) from global
+// to this CTA's shared memory; completion is counted on `bar`.
+__device__ __forceinline__ void bulk_load(void *dst_smem, const void *src_gmem, uint32_t bytes,
+                                          uint64_t *bar)
+{
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::
+            "r"(smem_u32(dst_smem)),
+        "l"(src_gmem), "r"(bytes), "r"(smem_u32(bar))
+        : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity)
+{
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+        " selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// Bounded wait for phase `parity` of `bar`.  On expiry the error word gets
+// XSS_DEVERR_TIMEOUT and the wait continues for a second bounded period so
+// that the copy in flight normally still lands before the buffer is reused;
+// after that the caller proceeds (results are then flagged invalid).
+__device__ __forceinline__ void mbar_wait_bounded(uint64_t *bar, uint32_t parity, unsigned *err)
+{
+    uint32_t spins = 0;
+    while (!mbar_try_wait(bar, parity)) {
+        if (++spins == XSS_SPIN_LIMIT) atomicOr(err, XSS_DEVERR_TIMEOUT);
+        if (spins >= 2 * XSS_SPIN_LIMIT) break;
+    }
+}
+
+}  // namespace xss

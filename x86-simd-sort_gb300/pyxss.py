@@ -18,7 +18,8 @@ import os
 import numpy as np
 
 PKG_DIR = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(PKG_DIR, "libxss_gb300.so")
+# XSS_LIB points at another build of the same library (e.g. a tuning variant)
+LIB_PATH = os.environ.get("XSS_LIB") or os.path.join(PKG_DIR, "libxss_gb300.so")
 
 DTYPES = {
     "uint16": 0, "int16": 1, "float16": 2,
