@@ -152,6 +152,30 @@ size_t xss_gpu_segmented_workspace_size(int key_dtype, int val_dtype,
                                         const uint64_t *h_offsets,
                                         size_t num_segments);
 
+/*
+ * Reusable plan for a fixed segment layout.  The segments are binned by size
+ * once (<= 32 keys: a warp each; <= 4096: a CTA each; larger: one segmented
+ * radix sort over all of them).  xss_seg_plan_run enqueues the whole batch on
+ * `stream`; with use_graph != 0 the launch sequence is captured into a CUDA
+ * graph on the first run and replayed while keys, values, offsets and
+ * workspace stay the same pointers.  val_dtype < 0: keys only.  A plan is not
+ * safe to run from two host threads at once.
+ */
+typedef struct xss_seg_plan_s *xss_seg_plan;
+int xss_seg_plan_create(xss_seg_plan *out, int key_dtype, int val_dtype,
+                        const uint64_t *h_offsets, size_t num_segments, int hasnan,
+                        int descending);
+size_t xss_seg_plan_workspace_size(const struct xss_seg_plan_s *plan);
+int xss_seg_plan_run(xss_seg_plan plan, void *d_keys, void *d_vals, const uint64_t *d_offsets,
+                     void *d_ws, size_t ws_bytes, xss_stream_t stream, int use_graph);
+void xss_seg_plan_destroy(xss_seg_plan plan);
+
+/* The same batch sorted by one single-array call per segment (the baseline
+ * the batched form is measured against). */
+int xss_gpu_segmented_sort_percall(int key_dtype, int val_dtype, void *d_keys, void *d_vals,
+                                   const uint64_t *h_offsets, size_t num_segments, int hasnan,
+                                   int descending, xss_stream_t stream);
+
 /* ------------------------------------------------------------------ */
 /* Instrumentation: per-kernel-kind launch counts (always on) and       */
 /* optional CUDA-event timing of every launch on its own stream.        */

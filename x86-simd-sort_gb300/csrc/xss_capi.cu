@@ -81,7 +81,7 @@ struct WsEntry {
 };
 static std::map<std::pair<int, cudaStream_t>, WsEntry> g_ws;
 
-static int cached_workspace(cudaStream_t s, size_t bytes, void **out)
+int cached_workspace(cudaStream_t s, size_t bytes, void **out)
 {
     *out = nullptr;
     if (bytes == 0) return XSS_OK;

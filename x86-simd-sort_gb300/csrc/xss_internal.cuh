@@ -9,6 +9,9 @@
 
 namespace xss {
 
+// Value type of a keys-only sort.
+struct NoVal {};
+
 // Operation families understood by the sort engine.
 enum SortOp : int { SOP_KEYS = 0, SOP_KV = 1, SOP_ARG = 2 };
 
@@ -82,6 +85,9 @@ int radix_select(int op, int kbytes, KeyXform xf, void *keys, void *vals, int vb
                  cudaStream_t s);
 
 int num_sms();
+
+// Library-owned scratch for (current device, stream), grown on demand.
+int cached_workspace(cudaStream_t s, size_t bytes, void **out);
 
 }  // namespace xss
 

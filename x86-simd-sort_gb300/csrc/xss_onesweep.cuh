@@ -16,8 +16,6 @@
 
 namespace xss {
 
-struct NoVal {};
-
 // Block-wide exclusive scan of one 32-bit value per thread.
 template <int BLOCK>
 __device__ __forceinline__ uint32_t block_excl_scan(uint32_t v, uint32_t *s_warp,
@@ -105,21 +103,22 @@ template <typename C, typename V> constexpr size_t pass_tile_size()
 #define XSS_LOOKBACK_FIRST 16
 #endif
 template <int LB>
-__device__ __forceinline__ uint32_t lookback_excl(const uint32_t *st_pass, uint32_t tile, int d,
-                                                  unsigned *err)
+__device__ __forceinline__ uint32_t lookback_excl(const uint32_t *st_pass, uint32_t tile,
+                                                  uint32_t first, int d, unsigned *err)
 {
     uint32_t excl = 0;
     int p = (int)tile - 1;
+    const int lo = (int)first;
     uint32_t spins = 0;
     // the first round probes only the nearest predecessors; later rounds LB
     int width = XSS_LOOKBACK_FIRST < LB ? XSS_LOOKBACK_FIRST : LB;
-    while (p >= 0) {
+    while (p >= lo) {
         uint32_t v[LB];
 #pragma unroll
         for (int w = 0; w < LB; ++w)
-            v[w] = (w < width && p - w >= 0)
+            v[w] = (w < width && p - w >= lo)
                        ? ld_relaxed_u32(st_pass + (size_t)(p - w) * RADIX + d)
-                       : (p - w >= 0 ? 0u : FLAG_PRE);
+                       : (p - w >= lo ? 0u : FLAG_PRE);
         int used = 0;
         bool done = false;
 #pragma unroll
@@ -150,6 +149,18 @@ template <int BLOCK> struct PassSmem {
     uint32_t scan[BLOCK / 32];
 };
 
+// Where a tile sits: its row in the look-back status array, the first tile
+// of its segment (a whole-array sort has one segment), its first element and
+// the segment's size, and this pass's bucket starts relative to the segment.
+struct TileJob {
+    uint32_t tile;
+    uint32_t first;
+    uint32_t base;
+    uint32_t n;
+    const uint32_t *start;
+    uint32_t *st_pass;      // this pass's look-back status rows
+};
+
 // Rank, publish, look up offsets and scatter one tile whose keys (codes) and
 // values are in registers.  s_k / s_v: TILE-sized staging buffers that no
 // thread reads any more once the first barrier here is passed.
@@ -159,7 +170,7 @@ template <int BLOCK> struct PassSmem {
 template <typename C, typename V, int BLOCK, int ITEMS, int LB, int RANK, typename VS,
           typename AfterRank>
 __device__ __forceinline__ void pass_tile(const RadixArgs &a, const PassDesc &pd, int pass,
-                                          uint32_t tile, const C (&key)[ITEMS],
+                                          const TileJob &job, const C (&key)[ITEMS],
                                           const VS (&val)[ITEMS], C *s_k, VS *s_v,
                                           PassSmem<BLOCK> &ps, C *kdst, V *vdst,
                                           AfterRank after_rank)
@@ -168,9 +179,10 @@ __device__ __forceinline__ void pass_tile(const RadixArgs &a, const PassDesc &pd
     constexpr int TILE = BLOCK * ITEMS;
     constexpr bool HAS_V = !std::is_same<V, NoVal>::value;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const uint32_t n = (uint32_t)a.n;
+    const uint32_t n = job.n;
+    const uint32_t tile = job.tile;
     const int shift = pass * RADIX_BITS;
-    const uint32_t tile_base = tile * (uint32_t)TILE;
+    const uint32_t tile_base = job.base;
     uint32_t *wh = ps.whist + warp * RADIX;
 
     // ---- per-warp digit counts (independent shared atomics)
@@ -180,12 +192,12 @@ __device__ __forceinline__ void pass_tile(const RadixArgs &a, const PassDesc &pd
 
     // ---- tile counts published at once, so successors' look-backs can pass
     // this tile; then each warp's exclusive offset per digit
-    uint32_t *st_tile = a.status + ((size_t)pass * a.num_tiles + tile) * RADIX;
+    uint32_t *st_tile = job.st_pass + (size_t)tile * RADIX;
     uint32_t cnt = 0;
     if (tid < RADIX) {
 #pragma unroll
         for (int w = 0; w < WARPS; ++w) cnt += ps.whist[w * RADIX + tid];
-        st_relaxed_u32(st_tile + tid, (tile == 0 ? FLAG_PRE : FLAG_AGG) | cnt);
+        st_relaxed_u32(st_tile + tid, (tile == job.first ? FLAG_PRE : FLAG_AGG) | cnt);
     }
     uint32_t total;
     const uint32_t local_start = block_excl_scan<BLOCK>(cnt, ps.scan, total);
@@ -245,12 +257,11 @@ __device__ __forceinline__ void pass_tile(const RadixArgs &a, const PassDesc &pd
     // ---- look-back for this tile's global offsets
     if (tid < RADIX) {
         uint32_t excl = 0;
-        if (tile > 0) {
-            excl = lookback_excl<LB>(a.status + (size_t)pass * a.num_tiles * RADIX, tile, tid,
-                                     a.err);
+        if (tile > job.first) {
+            excl = lookback_excl<LB>(job.st_pass, tile, job.first, tid, a.err);
             st_relaxed_u32(st_tile + tid, FLAG_PRE | ((excl + cnt) & COUNT_MASK));
         }
-        ps.off[tid] = (int32_t)(a.hdr->start[pass][tid] + excl) - (int32_t)local_start;
+        ps.off[tid] = (int32_t)(job.start[tid] + excl) - (int32_t)local_start;
     }
     __syncthreads();
 
@@ -333,7 +344,9 @@ __global__ void __launch_bounds__(BLOCK, MINB) onesweep_kernel(RadixArgs a, int 
             val[j] = pd.gen_idx ? VS(idx) : (idx < n ? vsrc[idx] : VS(0));
         }
     }
-    pass_tile<C, V, BLOCK, ITEMS, LB, RANK>(a, pd, pass, tile, key, val, s_k, s_v, ps,
+    const TileJob job{tile, 0u, tile * (uint32_t)TILE, n, a.hdr->start[pass],
+                      a.status + (size_t)pass * a.num_tiles * RADIX};
+    pass_tile<C, V, BLOCK, ITEMS, LB, RANK>(a, pd, pass, job, key, val, s_k, s_v, ps,
                                       static_cast<C *>(pick3(a.kbuf, pd.dst)), vdst,
                                       NoAfterRank{});
 }
@@ -461,7 +474,9 @@ __global__ void __launch_bounds__(BLOCK, MINB) onesweep_persist_kernel(RadixArgs
                 }
             }
         };
-        pass_tile<C, V, BLOCK, ITEMS, LB, RANK>(a, pd, pass, tile, key, val, s_k, s_v, ps, kdst, vdst,
+        const TileJob job{tile, 0u, tile_base, n, a.hdr->start[pass],
+                          a.status + (size_t)pass * num_tiles * RADIX};
+        pass_tile<C, V, BLOCK, ITEMS, LB, RANK>(a, pd, pass, job, key, val, s_k, s_v, ps, kdst, vdst,
                                           claim_next);
         __syncthreads();
     }

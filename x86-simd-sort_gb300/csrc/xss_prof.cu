@@ -40,6 +40,12 @@ static cudaEvent_t take_event()
 void prof_begin(cudaStream_t s, int kind)
 {
     if (!g_prof_on.load(std::memory_order_relaxed)) return;
+    // launches being captured into a graph are counted, not timed
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(s, &cap) != cudaSuccess || cap != cudaStreamCaptureStatusNone) {
+        cudaGetLastError();
+        return;
+    }
     std::lock_guard<std::mutex> lk(g_prof_mu);
     cudaEvent_t e = take_event();
     cudaEventRecord(e, s);

@@ -14,6 +14,7 @@
 #include <cstring>
 #include <mutex>
 #include <type_traits>
+#include "xss_blocksort.cuh"
 #include "xss_onesweep.cuh"
 
 namespace xss {
@@ -147,82 +148,6 @@ __global__ void fixup_kernel(RadixArgs a)
 }
 
 // ---------------------------------------------------------------------------
-// Small inputs: one CTA, bitonic network in shared memory over (code, index)
-// pairs.  The index tie-break makes the network stable and lets values and
-// argsort indices follow the keys by one gather.  Replaces the reference's
-// register networks for n <= network_sort_threshold
-// (src/xss-network-qsort.hpp:171-234, src/xss-network-keyvaluesort.hpp:209-388).
-struct SmallArgs {
-    const void *keys_in;
-    void *keys_out;      // nullptr: keys not written (argsort)
-    const void *vals_in;
-    void *vals_out;
-    uint64_t *out_idx;   // argsort output
-    uint32_t n, npad;
-    KeyXform xf;
-};
-
-constexpr int SMALL_BLOCK = 1024;
-
-template <typename C, typename V>
-__global__ void __launch_bounds__(SMALL_BLOCK) small_sort_kernel(SmallArgs a)
-{
-    constexpr bool HAS_V = !std::is_same<V, NoVal>::value;
-    extern __shared__ __align__(16) unsigned char s_raw[];
-    C *s_code = reinterpret_cast<C *>(s_raw);
-    uint16_t *s_idx = reinterpret_cast<uint16_t *>(s_raw + sizeof(C) * a.npad);
-    const int tid = threadIdx.x;
-    const uint32_t n = a.n, npad = a.npad;
-    const C *kin = static_cast<const C *>(a.keys_in);
-    for (uint32_t i = tid; i < npad; i += SMALL_BLOCK) {
-        s_code[i] = i < n ? to_code(kin[i], a.xf) : C(~C(0));
-        s_idx[i] = (uint16_t)i;
-    }
-    __syncthreads();
-    for (uint32_t k = 2; k <= npad; k <<= 1) {
-        for (uint32_t j = k >> 1; j > 0; j >>= 1) {
-            for (uint32_t t = tid; t < npad / 2; t += SMALL_BLOCK) {
-                const uint32_t i = 2 * t - (t & (j - 1));
-                const uint32_t ixj = i + j;
-                const C ca = s_code[i], cb = s_code[ixj];
-                const uint16_t ia = s_idx[i], ib = s_idx[ixj];
-                const bool a_gt_b = (ca > cb) || (ca == cb && ia > ib);
-                const bool up = (i & k) == 0;
-                if (a_gt_b == up) {
-                    s_code[i] = cb; s_code[ixj] = ca;
-                    s_idx[i] = ib;  s_idx[ixj] = ia;
-                }
-            }
-            __syncthreads();
-        }
-    }
-    if (a.keys_out) {
-        C *kout = static_cast<C *>(a.keys_out);
-        for (uint32_t i = tid; i < n; i += SMALL_BLOCK) kout[i] = from_code(s_code[i], a.xf);
-    }
-    if (a.out_idx) {
-        for (uint32_t i = tid; i < n; i += SMALL_BLOCK) a.out_idx[i] = s_idx[i];
-    }
-    if constexpr (HAS_V) {
-        constexpr int R = (int)(SMALL_SORT_MAX / SMALL_BLOCK);
-        const V *vin = static_cast<const V *>(a.vals_in);
-        V tmp[R];
-#pragma unroll
-        for (int r = 0; r < R; ++r) {
-            const uint32_t i = tid + r * SMALL_BLOCK;
-            if (i < n) tmp[r] = vin[s_idx[i]];
-        }
-        __syncthreads();
-        V *vout = static_cast<V *>(a.vals_out);
-#pragma unroll
-        for (int r = 0; r < R; ++r) {
-            const uint32_t i = tid + r * SMALL_BLOCK;
-            if (i < n) vout[i] = tmp[r];
-        }
-    }
-}
-
-// ---------------------------------------------------------------------------
 // Host side.
 struct RadixLayout {
     size_t hdr, status, k1, k2, v1, v2, total;
@@ -293,7 +218,8 @@ static int small_sort_launch(int op, KeyXform xf, void *keys, void *vals,
     a.npad = npad;
     a.xf = xf;
     const size_t smem = align_up(sizeof(C) * npad, 16) + 2 * npad;  // <= 40 KiB
-    XSS_LAUNCH_OPT(o, PK_SMALL, s, small_sort_kernel<C, V><<<1, SMALL_BLOCK, smem, s>>>(a));
+    XSS_LAUNCH_OPT(o, PK_SMALL, s,
+                   (small_sort_kernel<C, V, SMALL_BLOCK, SMALL_SORT_MAX><<<1, SMALL_BLOCK, smem, s>>>(a)));
     XSS_CUDA_TRY(cudaGetLastError());
     return XSS_OK;
 }

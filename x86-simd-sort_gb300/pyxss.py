@@ -67,6 +67,11 @@ _SIGS = {
     "xss_keyvalue_qsort": (_I, [_I, _I, _P, _P, _Z, _I, _I]),
     "xss_keyvalue_select": (_I, [_I, _I, _P, _P, _Z, _Z, _I, _I]),
     "xss_keyvalue_partial_sort": (_I, [_I, _I, _P, _P, _Z, _Z, _I, _I]),
+    "xss_seg_plan_create": (_I, [ctypes.POINTER(_P), _I, _I, _P, _Z, _I, _I]),
+    "xss_seg_plan_workspace_size": (_Z, [_P]),
+    "xss_seg_plan_run": (_I, [_P, _P, _P, _P, _P, _Z, _P, _I]),
+    "xss_seg_plan_destroy": (None, [_P]),
+    "xss_gpu_segmented_sort_percall": (_I, [_I, _I, _P, _P, _P, _Z, _I, _I, _P]),
     "xss_prof_enable": (None, [_I]),
     "xss_prof_reset": (None, []),
     "xss_prof_read": (_I, [_I, ctypes.POINTER(ctypes.c_double),
@@ -260,3 +265,42 @@ def gpu_segmented_sort(kdt, vdt, d_keys, d_vals, d_offsets, h_offsets: np.ndarra
 def segmented_workspace_size(kdt, vdt, h_offsets: np.ndarray) -> int:
     return lib().xss_gpu_segmented_workspace_size(dtype_id(kdt), dtype_id(vdt) if vdt else -1,
                                                   _ptr(h_offsets), h_offsets.size - 1)
+
+
+def gpu_segmented_sort_percall(kdt, vdt, d_keys, d_vals, h_offsets: np.ndarray, hasnan=False,
+                               descending=False, stream=0):
+    check(lib().xss_gpu_segmented_sort_percall(dtype_id(kdt), dtype_id(vdt) if vdt else -1,
+                                               d_keys, d_vals or None, _ptr(h_offsets),
+                                               h_offsets.size - 1, int(hasnan), int(descending),
+                                               stream or None), "segmented_sort_percall")
+
+
+class SegPlan:
+    """A reusable segmented-sort plan (xss_seg_plan_*) for one offsets layout."""
+
+    def __init__(self, kdt, vdt, h_offsets: np.ndarray, hasnan=False, descending=False):
+        self._h = ctypes.c_void_p()
+        self._off = np.ascontiguousarray(h_offsets, dtype=np.uint64)
+        check(lib().xss_seg_plan_create(ctypes.byref(self._h), dtype_id(kdt),
+                                        dtype_id(vdt) if vdt else -1, _ptr(self._off),
+                                        self._off.size - 1, int(hasnan), int(descending)),
+              "seg_plan_create")
+
+    @property
+    def workspace_size(self) -> int:
+        return lib().xss_seg_plan_workspace_size(self._h)
+
+    def run(self, d_keys, d_vals, d_offsets, ws, ws_bytes, stream=0, use_graph=True):
+        check(lib().xss_seg_plan_run(self._h, d_keys, d_vals or None, d_offsets, ws, ws_bytes,
+                                     stream or None, int(use_graph)), "seg_plan_run")
+
+    def close(self):
+        if self._h:
+            lib().xss_seg_plan_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
