@@ -52,6 +52,23 @@ void prof_begin(cudaStream_t s, int kind)
     t_open[kind] = e;
 }
 
+void prof_snapshot(unsigned long long *out)
+{
+    for (int k = 0; k < PK_COUNT; ++k) out[k] = g_launches[k].load();
+}
+
+void prof_add(const unsigned long long *counts)
+{
+    for (int k = 0; k < PK_COUNT; ++k)
+        if (counts[k]) g_launches[k].fetch_add(counts[k], std::memory_order_relaxed);
+}
+
+void prof_sub(const unsigned long long *counts)
+{
+    for (int k = 0; k < PK_COUNT; ++k)
+        if (counts[k]) g_launches[k].fetch_sub(counts[k], std::memory_order_relaxed);
+}
+
 void prof_end(cudaStream_t s, int kind)
 {
     g_launches[kind].fetch_add(1, std::memory_order_relaxed);

@@ -21,5 +21,10 @@ enum ProfKind : int {
 
 void prof_begin(cudaStream_t s, int kind);
 void prof_end(cudaStream_t s, int kind);
+// Snapshot of the per-kind launch counters (PK_COUNT entries), and a bulk
+// add -- used to count kernels that run inside a replayed CUDA graph.
+void prof_snapshot(unsigned long long *out);
+void prof_add(const unsigned long long *counts);
+void prof_sub(const unsigned long long *counts);
 
 }  // namespace xss

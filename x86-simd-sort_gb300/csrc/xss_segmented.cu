@@ -242,6 +242,7 @@ struct SegPlan {
     cudaGraphExec_t exec = nullptr;
     const void *gk = nullptr, *gv = nullptr, *goff = nullptr, *gws = nullptr;
     const void *uploaded_to = nullptr;  // workspace that holds this plan's lists
+    unsigned long long graph_launches[PK_COUNT] = {};  // kernels per graph replay, by kind
 };
 
 static size_t seg_tile_size(int kb, int vb)
@@ -555,7 +556,14 @@ int xss_seg_plan_run(xss_seg_plan_s *plan, void *d_keys, void *d_vals, const uin
         if (cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
             rc = XSS_ECUDA;
         } else {
+            // launches issued while capturing did not run: move them from the
+            // counters into the per-replay count
+            unsigned long long before[PK_COUNT], after[PK_COUNT];
+            prof_snapshot(before);
             rc = plan_enqueue(p, d_keys, d_vals, d_offsets, cs);
+            prof_snapshot(after);
+            for (int k = 0; k < PK_COUNT; ++k) p.graph_launches[k] = after[k] - before[k];
+            prof_sub(p.graph_launches);
             if (cudaStreamEndCapture(cs, &g) != cudaSuccess) rc = rc ? rc : XSS_ECUDA;
         }
         if (rc == XSS_OK && cudaGraphInstantiate(&p.exec, g, 0) != cudaSuccess) rc = XSS_ECUDA;
@@ -572,6 +580,7 @@ int xss_seg_plan_run(xss_seg_plan_s *plan, void *d_keys, void *d_vals, const uin
         p.gws = d_ws;
     }
     XSS_CUDA_TRY(cudaGraphLaunch(p.exec, s));
+    prof_add(p.graph_launches);
     return XSS_OK;
 }
 
