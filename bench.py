@@ -448,12 +448,162 @@ def reference_arm(args):
     print(json.dumps(line), flush=True)
 
 
+def run_serving(args):
+    """Serving loop under Poisson load (offered 20k req/s by default).
+
+    Mix: 45% qsort, 25% argsort, 20% qselect (k uniform in [0, n)), 10%
+    keyvalue_qsort; sizes log-uniform in [2^10, 2^26]; key types uniform over
+    {float32, int64, float16, float64, uint32} (32/64-bit only for key-value);
+    float keys ~ N(0,1) with 0.1% NaN, hasnan = true; seed 4.  Inputs are read
+    from shared pinned source arrays, results land in a pinned output ring; a
+    request that finds the ring or the server queue full is shed."""
+    import torch
+    import pyxss as xss
+    torch.cuda.set_device(0)
+    rng = np.random.default_rng(4)
+    nmax = 1 << 26
+    dts = ["float32", "int64", "float16", "float64", "uint32"]
+    src = {}
+    for dt in dts:
+        d = np.dtype(dt)
+        t = torch.empty(nmax * d.itemsize, dtype=torch.uint8, pin_memory=True)
+        a = t.numpy().view(d)
+        if d.kind == "f":
+            a[:] = rng.standard_normal(nmax).astype(d)
+            a[rng.random(nmax) < 0.001] = np.nan
+        else:
+            a[:] = rng.integers(np.iinfo(d).min, np.iinfo(d).max, nmax, dtype=d, endpoint=True)
+        src[dt] = (t, a)
+    vt = torch.empty(nmax * 8, dtype=torch.uint8, pin_memory=True)
+    vsrc = vt.numpy().view(np.uint64)
+    vsrc[:] = np.arange(nmax, dtype=np.uint64)
+    ring_bytes = args.ring_gb << 30
+    ring_t = torch.empty(ring_bytes, dtype=torch.uint8, pin_memory=True)
+    ring = ring_t.numpy()
+    srv = xss.Server(hbm_budget_bytes=args.serve_budget_gb << 30, small_max=1 << 14,
+                     max_queue=args.serve_queue, streams=args.serve_streams)
+    peak, peak_src = _peaks()
+
+    head = tail = 0          # ring bytes [tail, head) are in use, FIFO order
+    inflight = []            # (ticket, ring_end, bytes_model, check)
+    offered = shed_client = submitted = 0
+    model_bytes_done = 0
+    t_start = time.perf_counter()
+    t_next = t_start
+    deadline = t_start + args.duration
+    samples = []
+    while True:
+        now = time.perf_counter()
+        # retire finished requests in FIFO order to free ring space
+        while inflight:
+            st = srv.poll(inflight[0][0])
+            if st is None:
+                break
+            tk, end, mb, chk = inflight.pop(0)
+            assert st == 0, st
+            tail = end
+            model_bytes_done += mb
+            if chk is not None and len(samples) < 64:
+                samples.append(chk())
+        if not inflight:
+            head = tail = 0
+        if now >= deadline:
+            break
+        if now < t_next:
+            time.sleep(min(t_next - now, 200e-6))
+            continue
+        t_next += rng.exponential(1.0 / args.rate)
+        offered += 1
+        u = rng.random()
+        op = ("qsort" if u < 0.45 else "argsort" if u < 0.70 else "qselect" if u < 0.90
+              else "keyvalue_qsort")
+        dt = dts[rng.integers(0, len(dts))]
+        if op == "keyvalue_qsort" and dt == "float16":
+            dt = "float32"
+        n = int(2.0 ** rng.uniform(10, 26))
+        kb = np.dtype(dt).itemsize
+        out_b = n * (8 if op == "argsort" else kb) + (n * 8 if op == "keyvalue_qsort" else 0)
+        out_b = (out_b + 255) // 256 * 256
+        if out_b > ring_bytes - head:
+            if tail >= out_b and not inflight:
+                head = tail = 0
+            shed_client += 1
+            continue
+        o = head
+        head += out_b
+        a = src[dt][1]
+        kw = dict(n=n, hasnan=np.dtype(dt).kind == "f")
+        pout = ring[o:].ctypes.data
+        if op == "argsort":
+            t = srv.submit(op, dt, a.ctypes.data, None, arg_out=pout, **kw)
+            mb = n * (kb + 2 * kb * (kb + 8)) - n * (8 + kb)
+        elif op == "keyvalue_qsort":
+            t = srv.submit(op, dt, a.ctypes.data, pout, vals_in=vsrc.ctypes.data,
+                           vals_out=pout + n * kb, val_dtype="uint64", **kw)
+            mb = n * (kb + 2 * kb * (kb + 8))
+        elif op == "qselect":
+            t = srv.submit(op, dt, a.ctypes.data, pout, k=int(rng.integers(0, n)), **kw)
+            mb = 3 * n * kb
+        else:
+            t = srv.submit(op, dt, a.ctypes.data, pout, **kw)
+            mb = n * kb * (1 + 2 * kb)
+        if t is None:
+            head -= out_b
+            continue
+        submitted += 1
+        chk = None
+        if op == "qsort" and n <= (1 << 16) and len(samples) < 64:
+            view = ring[o:o + n * kb].view(np.dtype(dt))
+            base = a[:n].copy()
+            chk = (lambda v=view, b=base, d=dt: bool(np.array_equal(
+                np.isnan(v) if np.dtype(d).kind == "f" else v,
+                np.isnan(np.sort(b)) if np.dtype(d).kind == "f" else np.sort(b))))
+        inflight.append((t, head, mb, chk))
+    for tk, end, mb, chk in inflight:
+        assert srv.wait(tk) == 0
+        model_bytes_done += mb
+    wall = time.perf_counter() - t_start
+    st = srv.stats()
+    srv.close()
+    shed_total = shed_client + st["shed"]
+    line = {
+        "metric": "serving Gkeys/s with p50/p99 latency", "value": st["keys"] / wall / 1e9,
+        "unit": "Gkeys/s", "n_gpus": 1, "steps": 1, "warmup": 0, "ms_per_step": wall * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "mixed",
+        "data": "synthetic (seeded Poisson arrivals, seed 4)",
+        "config": {"workload": "serving loop", "offered_req_per_s": args.rate,
+                   "duration_s": args.duration, "mix": "45% qsort, 25% argsort, 20% qselect, "
+                   "10% keyvalue_qsort", "sizes": "log-uniform [2^10, 2^26]",
+                   "dtypes": dts, "hbm_pool_gb": args.serve_budget_gb,
+                   "ring_gb": args.ring_gb, "streams": args.serve_streams,
+                   "queue_limit": args.serve_queue},
+        "serving": {"offered": offered, "submitted": submitted,
+                    "shed": shed_total, "shed_fraction": shed_total / max(offered, 1),
+                    "completed": st["completed"], "failed": st["failed"],
+                    "completed_req_per_s": st["completed"] / wall,
+                    "batches": st["batches"], "batched_requests": st["batched_requests"],
+                    "p50_ms": st["p50_us"] / 1e3, "p99_ms": st["p99_us"] / 1e3,
+                    "max_ms": st["max_us"] / 1e3,
+                    "hbm_frac_model": model_bytes_done / wall / 1e9 / peak,
+                    "peak_source": peak_src,
+                    "checked_samples": len(samples), "checked_ok": all(samples)},
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
-    ap.add_argument("--workload", default="keyvalue_qsort", choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default="keyvalue_qsort",
+                    choices=sorted(WORKLOADS) + ["serving"])
+    ap.add_argument("--rate", type=float, default=20000.0, help="serving: offered req/s")
+    ap.add_argument("--duration", type=float, default=2.0, help="serving: seconds of arrivals")
+    ap.add_argument("--ring-gb", type=int, default=16, help="serving: pinned output ring")
+    ap.add_argument("--serve-budget-gb", type=int, default=64, help="serving: device pool")
+    ap.add_argument("--serve-streams", type=int, default=4, help="serving: request streams")
+    ap.add_argument("--serve-queue", type=int, default=32, help="serving: queue limit")
     ap.add_argument("--n", type=int, default=0, help="override the array size")
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-sample", type=int, default=1 << 24)
@@ -462,6 +612,9 @@ def main():
     args = ap.parse_args()
     assert args.warmup >= 3 or args.impl == "reference", "at least 3 warm-up steps"
 
+    if args.workload == "serving" and args.impl == "ours":
+        run_serving(args)
+        return
     if args.impl == "reference":
         reference_arm(args)
         return

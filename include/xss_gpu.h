@@ -37,7 +37,9 @@ enum {
     XSS_ETIMEOUT = 3,    /* a bounded device-side wait gave up (result invalid) */
     XSS_ECUDA = 4,       /* a CUDA runtime call failed */
     XSS_EUNSUPPORTED = 5,/* type combination the reference does not offer */
-    XSS_ETOOBIG = 6      /* n above the library limit (XSS_MAX_N) */
+    XSS_ETOOBIG = 6,     /* n above the library limit (XSS_MAX_N) */
+    XSS_EBUSY = 7,       /* server queue full or stopping: request refused */
+    XSS_EAGAIN = 8       /* server request not finished yet */
 };
 
 /* Largest array the device kernels accept (tile look-back counters are 30-bit). */
@@ -188,6 +190,57 @@ void xss_prof_reset(void);
 int xss_prof_read(int kind, double *total_ms, unsigned long long *timed_launches);
 unsigned long long xss_prof_launches(int kind);
 const char *xss_prof_kind_name(int kind);
+
+/* ------------------------------------------------------------------ */
+/* Serving loop: a scheduler thread that takes sort / select / argsort / */
+/* key-value requests on host buffers, admits them as device memory for */
+/* their data and scratch frees up (continuous batching), coalesces     */
+/* small same-kind requests into one segmented sort, runs large ones on */
+/* a pool of streams so their copies and kernels overlap, and keeps     */
+/* arrival-to-completion latencies.  Host buffers should be pinned for  */
+/* the copies to overlap.  No counterpart in the reference library.     */
+/* ------------------------------------------------------------------ */
+typedef struct xss_serve_request {
+    int op;                 /* XSS_OP_* */
+    int key_dtype, val_dtype;
+    const void *keys_in;    /* n keys (host) */
+    void *keys_out;         /* result keys (may equal keys_in); unused for arg ops */
+    const void *vals_in;    /* key-value ops */
+    void *vals_out;
+    uint64_t *arg_out;      /* argsort / argselect: n indices */
+    size_t n, k;
+    int hasnan, descending;
+} xss_serve_request;
+
+typedef struct xss_server_config {
+    int device;
+    size_t hbm_budget_bytes;  /* device pool for data + scratch; 0: half of free memory */
+    int streams;              /* streams for large requests; 0: 4 */
+    size_t small_max;         /* requests up to this size are coalesced; 0: 65536 */
+    size_t max_batch;         /* requests per coalesced launch; 0: 4096 */
+    size_t max_queue;         /* queued requests before submissions are refused; 0: 1024 */
+} xss_server_config;
+
+typedef struct xss_server_stats {
+    uint64_t submitted, shed, completed, failed, batches, batched_requests;
+    double keys;              /* keys in completed requests */
+    double wall_s;            /* since creation or the last reset */
+    double p50_us, p99_us, max_us;  /* arrival -> completion */
+    size_t pool_bytes;
+} xss_server_stats;
+
+typedef struct xss_server_s *xss_server;
+int xss_server_create(xss_server *out, const xss_server_config *cfg);
+/* XSS_OK and a ticket, or XSS_EBUSY when the queue is full (request shed). */
+int xss_server_submit(xss_server s, const xss_serve_request *req, uint64_t *ticket);
+/* Block until the request is done; *status is its result code. */
+int xss_server_wait(xss_server s, uint64_t ticket, int *status);
+/* XSS_OK with *status when done, XSS_EAGAIN while pending. */
+int xss_server_poll(xss_server s, uint64_t ticket, int *status);
+int xss_server_get_stats(xss_server s, xss_server_stats *out);
+int xss_server_reset_stats(xss_server s);
+/* Stop admitting; drain != 0 finishes queued work, else refuses it (XSS_EBUSY). */
+void xss_server_destroy(xss_server s, int drain);
 
 /* ------------------------------------------------------------------ */
 /* Host-pointer entry points: copy in, run on the device, copy back.     */

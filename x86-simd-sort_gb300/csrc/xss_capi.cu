@@ -371,6 +371,8 @@ const char *xss_strerror(int status)
     case XSS_ECUDA: return "CUDA runtime error";
     case XSS_EUNSUPPORTED: return "unsupported type combination";
     case XSS_ETOOBIG: return "array larger than XSS_MAX_N";
+    case XSS_EBUSY: return "server busy: request refused";
+    case XSS_EAGAIN: return "request still pending";
     default: return "unknown status";
     }
 }

@@ -304,3 +304,87 @@ class SegPlan:
             self.close()
         except Exception:
             pass
+
+
+# ---- serving loop -----------------------------------------------------------------
+class ServeRequest(ctypes.Structure):
+    _fields_ = [("op", _I), ("key_dtype", _I), ("val_dtype", _I), ("keys_in", _P),
+                ("keys_out", _P), ("vals_in", _P), ("vals_out", _P), ("arg_out", _P),
+                ("n", _Z), ("k", _Z), ("hasnan", _I), ("descending", _I)]
+
+
+class ServerConfig(ctypes.Structure):
+    _fields_ = [("device", _I), ("hbm_budget_bytes", _Z), ("streams", _I), ("small_max", _Z),
+                ("max_batch", _Z), ("max_queue", _Z)]
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [("submitted", ctypes.c_uint64), ("shed", ctypes.c_uint64),
+                ("completed", ctypes.c_uint64), ("failed", ctypes.c_uint64),
+                ("batches", ctypes.c_uint64), ("batched_requests", ctypes.c_uint64),
+                ("keys", ctypes.c_double), ("wall_s", ctypes.c_double),
+                ("p50_us", ctypes.c_double), ("p99_us", ctypes.c_double),
+                ("max_us", ctypes.c_double), ("pool_bytes", _Z)]
+
+
+_SERVER_SIGS = {
+    "xss_server_create": (_I, [ctypes.POINTER(_P), ctypes.POINTER(ServerConfig)]),
+    "xss_server_submit": (_I, [_P, ctypes.POINTER(ServeRequest), ctypes.POINTER(ctypes.c_uint64)]),
+    "xss_server_wait": (_I, [_P, ctypes.c_uint64, ctypes.POINTER(_I)]),
+    "xss_server_poll": (_I, [_P, ctypes.c_uint64, ctypes.POINTER(_I)]),
+    "xss_server_get_stats": (_I, [_P, ctypes.POINTER(ServerStats)]),
+    "xss_server_reset_stats": (_I, [_P]),
+    "xss_server_destroy": (None, [_P, _I]),
+}
+
+
+class Server:
+    """xss_server_*: submit requests on (preferably pinned) host buffers."""
+
+    def __init__(self, device=0, hbm_budget_bytes=0, streams=0, small_max=0, max_batch=0,
+                 max_queue=0):
+        L = lib()
+        for name, (res, args) in _SERVER_SIGS.items():
+            f = getattr(L, name)
+            f.restype, f.argtypes = res, args
+        self._L = L
+        self._h = _P()
+        cfg = ServerConfig(device, hbm_budget_bytes, streams, small_max, max_batch, max_queue)
+        check(L.xss_server_create(ctypes.byref(self._h), ctypes.byref(cfg)), "server_create")
+
+    def submit(self, op, key_dtype, keys_in, keys_out=None, n=None, k=0, vals_in=None,
+               vals_out=None, val_dtype="uint64", arg_out=None, hasnan=False, descending=False):
+        """Returns a ticket, or None when the server refused the request (shed)."""
+        r = ServeRequest(OPS[op], dtype_id(key_dtype), dtype_id(val_dtype), keys_in,
+                         keys_out or keys_in, vals_in, vals_out or vals_in, arg_out, n, k,
+                         int(hasnan), int(descending))
+        t = ctypes.c_uint64(0)
+        rc = self._L.xss_server_submit(self._h, ctypes.byref(r), ctypes.byref(t))
+        if rc == 7:
+            return None
+        check(rc, "server_submit")
+        return t.value
+
+    def wait(self, ticket) -> int:
+        st = _I(0)
+        check(self._L.xss_server_wait(self._h, ticket, ctypes.byref(st)), "server_wait")
+        return st.value
+
+    def poll(self, ticket):
+        """Request status code, or None while it is pending."""
+        st = _I(0)
+        rc = self._L.xss_server_poll(self._h, ticket, ctypes.byref(st))
+        return None if rc == 8 else st.value
+
+    def stats(self) -> dict:
+        s = ServerStats()
+        check(self._L.xss_server_get_stats(self._h, ctypes.byref(s)), "server_stats")
+        return {name: getattr(s, name) for name, _ in ServerStats._fields_}
+
+    def reset_stats(self):
+        self._L.xss_server_reset_stats(self._h)
+
+    def close(self, drain=True):
+        if self._h:
+            self._L.xss_server_destroy(self._h, int(drain))
+            self._h = _P()
