@@ -448,6 +448,20 @@ def reference_arm(args):
     print(json.dumps(line), flush=True)
 
 
+def max_over_ranks(value: float, dist, device: str) -> float:
+    """The slowest rank's time: every rank gets the maximum over all ranks."""
+    import torch
+    t = torch.tensor([value], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_throughput(n_per_rank: int, ms_per_step: float, world: int) -> float:
+    """Gkeys/s of N independent replicas, each sorting n_per_rank keys per step,
+    timed by the slowest rank."""
+    return world * n_per_rank / (ms_per_step / 1e3) / 1e9
+
+
 def run_serving(args):
     """Serving loop under Poisson load (offered 20k req/s by default).
 
@@ -707,12 +721,10 @@ def main():
         percall = pc[-1]
 
     if dist is not None:
-        tt = torch.tensor([total_ms], device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        total_ms = float(tt.item())
+        total_ms = max_over_ranks(total_ms, dist, "cuda")
 
     ms_per_step = total_ms / args.steps
-    value = world * n / (ms_per_step / 1e3) / 1e9
+    value = replica_throughput(n, ms_per_step, world)
 
     peak, peak_src = _peaks()
     active = dom_launches / dom_steps if dom_launches else 0

@@ -78,6 +78,15 @@ size_t xss_gpu_workspace_size(int op, int key_dtype, int val_dtype, size_t n, si
  */
 int xss_gpu_stream_status(xss_stream_t stream);
 
+/*
+ * Self test of the device-side bounded waits: runs the look-back spin
+ * (which = 0) or the bulk-copy mbarrier wait (which = 1) against a condition
+ * that never becomes true, with the given spin limit.  Returns XSS_ETIMEOUT
+ * when the wait gave up as designed (synchronises `stream`).  Diagnostic
+ * only; no counterpart in the reference library.
+ */
+int xss_gpu_selftest_bounded_wait(int which, unsigned spin_limit, xss_stream_t stream);
+
 /* ------------------------------------------------------------------ */
 /* Device-pointer entry points.  Arrays live in device memory; work is   */
 /* enqueued on `stream`; the status of bounded waits is checked with a  */

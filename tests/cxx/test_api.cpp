@@ -1,0 +1,115 @@
+// C++ drop-in check: code written against the reference's x86simdsort.h
+// (lib/x86simdsort.h) compiles unchanged against include/x86simdsort.h and
+// gives std::sort's results, now computed on the GPU.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <random>
+#include <stdexcept>
+#include <vector>
+
+#include "x86simdsort.h"
+
+#define CHECK(c)                                                             \
+    do {                                                                     \
+        if (!(c)) {                                                          \
+            std::fprintf(stderr, "FAIL %s:%d: %s\n", __FILE__, __LINE__, #c); \
+            return 1;                                                        \
+        }                                                                    \
+    } while (0)
+
+struct Point {
+    double x, y;
+};
+
+int main()
+{
+    std::mt19937 gen(0);
+    std::uniform_real_distribution<float> uni(-1.0f, 1.0f);
+
+    // qsort<float>, ascending, 2^20 keys -- checked against std::sort
+    std::vector<float> a(1 << 20);
+    for (auto &v : a) v = uni(gen);
+    std::vector<float> b = a;
+    x86simdsort::qsort(a.data(), a.size());
+    std::sort(b.begin(), b.end());
+    CHECK(std::memcmp(a.data(), b.data(), a.size() * sizeof(float)) == 0);
+
+    // descending with NaN: the quiet NaN comes first
+    std::vector<double> d(100000);
+    std::normal_distribution<double> nd;
+    for (auto &v : d) v = nd(gen);
+    d[17] = std::nan("");
+    d[99] = std::nan("");
+    x86simdsort::qsort(d.data(), d.size(), true, true);
+    CHECK(std::isnan(d[0]) && std::isnan(d[1]) && !std::isnan(d[2]));
+    for (size_t i = 3; i < d.size(); ++i) CHECK(d[i - 1] >= d[i]);
+
+    // argsort<double>: a permutation whose gathered keys are sorted
+    std::vector<double> e(50000);
+    for (auto &v : e) v = nd(gen);
+    std::vector<size_t> arg = x86simdsort::argsort(e.data(), e.size());
+    std::vector<size_t> chk = arg;
+    std::sort(chk.begin(), chk.end());
+    for (size_t i = 0; i < chk.size(); ++i) CHECK(chk[i] == i);
+    for (size_t i = 1; i < arg.size(); ++i) CHECK(e[arg[i - 1]] <= e[arg[i]]);
+
+    // keyvalue_qsort<int64_t, uint64_t>
+    std::vector<int64_t> k(300000);
+    std::vector<uint64_t> v(k.size());
+    for (size_t i = 0; i < k.size(); ++i) {
+        k[i] = (int64_t)(gen() % 1000) - 500;
+        v[i] = i;
+    }
+    std::vector<int64_t> k0 = k;
+    x86simdsort::keyvalue_qsort(k.data(), v.data(), k.size());
+    for (size_t i = 1; i < k.size(); ++i) CHECK(k[i - 1] <= k[i]);
+    for (size_t i = 0; i < k.size(); ++i) CHECK(k0[v[i]] == k[i]);
+
+    // qselect / partial_qsort
+    std::vector<float> s = b;
+    std::shuffle(s.begin(), s.end(), gen);
+    std::vector<float> p = s;
+    x86simdsort::qselect(s.data(), 1000, s.size());
+    CHECK(s[1000] == b[1000]);
+    for (size_t i = 0; i < 1000; ++i) CHECK(s[i] <= s[1000]);
+    x86simdsort::partial_qsort(p.data(), 1000, p.size());
+    CHECK(std::memcmp(p.data(), b.data(), 1000 * sizeof(float)) == 0);
+
+    // object_qsort by member
+    std::vector<Point> objs(100000);
+    for (auto &o : objs) o = {nd(gen), nd(gen)};
+    std::vector<Point> ref = objs;
+    x86simdsort::object_qsort(objs.data(), objs.size(), [](Point q) { return q.x; });
+    std::sort(ref.begin(), ref.end(), [](const Point &l, const Point &r) { return l.x < r.x; });
+    for (size_t i = 0; i < objs.size(); ++i) CHECK(objs[i].x == ref[i].x && objs[i].y == ref[i].y);
+
+    // device-pointer overloads
+    float *d_arr = nullptr;
+    CHECK(cudaMalloc(&d_arr, a.size() * sizeof(float)) == cudaSuccess);
+    std::vector<float> c(a.size());
+    for (auto &x : c) x = uni(gen);
+    std::vector<float> cs = c;
+    std::sort(cs.begin(), cs.end(), std::greater<float>());
+    CHECK(cudaMemcpy(d_arr, c.data(), c.size() * 4, cudaMemcpyHostToDevice) == cudaSuccess);
+    x86simdsort::gpu::qsort(d_arr, c.size(), false, true);
+    x86simdsort::gpu::synchronize();
+    CHECK(cudaMemcpy(c.data(), d_arr, c.size() * 4, cudaMemcpyDeviceToHost) == cudaSuccess);
+    CHECK(c == cs);
+    cudaFree(d_arr);
+
+    // errors surface as exceptions (the reference has no error channel)
+    bool threw = false;
+    try {
+        x86simdsort::qselect(a.data(), a.size(), a.size());
+    } catch (const std::runtime_error &) {
+        threw = true;
+    }
+    CHECK(threw);
+
+    std::puts("cxx api ok");
+    return 0;
+}

@@ -104,7 +104,8 @@ template <typename C, typename V> constexpr size_t pass_tile_size()
 #endif
 template <int LB>
 __device__ __forceinline__ uint32_t lookback_excl(const uint32_t *st_pass, uint32_t tile,
-                                                  uint32_t first, int d, unsigned *err)
+                                                  uint32_t first, int d, unsigned *err,
+                                                  uint32_t spin_limit = XSS_SPIN_LIMIT)
 {
     uint32_t excl = 0;
     int p = (int)tile - 1;
@@ -131,7 +132,7 @@ __device__ __forceinline__ uint32_t lookback_excl(const uint32_t *st_pass, uint3
             if (f == FLAG_PRE) done = true;
         }
         if (done) return excl;
-        if (used == 0 && ++spins > XSS_SPIN_LIMIT) {
+        if (used == 0 && ++spins > spin_limit) {
             atomicOr(err, XSS_DEVERR_TIMEOUT);
             return excl;
         }

@@ -65,12 +65,13 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity)
 // XSS_DEVERR_TIMEOUT and the wait continues for a second bounded period so
 // that the copy in flight normally still lands before the buffer is reused;
 // after that the caller proceeds (results are then flagged invalid).
-__device__ __forceinline__ void mbar_wait_bounded(uint64_t *bar, uint32_t parity, unsigned *err)
+__device__ __forceinline__ void mbar_wait_bounded(uint64_t *bar, uint32_t parity, unsigned *err,
+                                                  uint32_t spin_limit = XSS_SPIN_LIMIT)
 {
     uint32_t spins = 0;
     while (!mbar_try_wait(bar, parity)) {
-        if (++spins == XSS_SPIN_LIMIT) atomicOr(err, XSS_DEVERR_TIMEOUT);
-        if (spins >= 2 * XSS_SPIN_LIMIT) break;
+        if (++spins == spin_limit) atomicOr(err, XSS_DEVERR_TIMEOUT);
+        if (spins >= 2 * spin_limit) break;
     }
 }
 
