@@ -373,9 +373,214 @@ class SegmentedSort(Workload):
         return int(self.off[stop])
 
 
+class QsortF32Small(QsortF32):
+    """qsort of 2^20 float32 keys (4 MiB, fits in L2): L2 is flushed between steps."""
+
+    name = "qsort_f32_2e20"
+    flush_l2 = True
+
+    def describe(self):
+        d = super().describe()
+        d["l2"] = "input fits in L2: a 256 MiB buffer is written between steps (untimed)"
+        return d
+
+
+class ArgsortWorkload(Workload):
+    """argsort at 2^28: int64 uniform full range ascending, or float64 ~ N(0,1)
+    with 1% quiet NaN and 0.5% +-0.0, hasnan, descending."""
+
+    name = "argsort"
+    kdt = "int64"
+    kb, ib = 8, 8
+    desc = False
+
+    def describe(self):
+        return {"workload": f"argsort {self.kdt} n=2^{self.n.bit_length() - 1}"
+                            + (" N(0,1) 1% NaN 0.5% +-0, hasnan, descending" if self.desc
+                               else " uniform full range, ascending"),
+                "n": self.n, "l2": "inputs larger than L2"}
+
+    def setup(self):
+        t, n = self.torch, self.n
+        g = t.Generator(device="cuda").manual_seed(1)
+        if self.kdt == "float64":
+            x = t.randn(n, dtype=t.float64, device="cuda", generator=g)
+            u = t.rand(n, dtype=t.float64, device="cuda", generator=g)
+            x[u < 0.01] = float("nan")
+            x[(u >= 0.01) & (u < 0.0125)] = 0.0
+            x[(u >= 0.0125) & (u < 0.015)] = -0.0
+            self.k0 = x
+        else:
+            self.k0 = t.randint(0, 256, (n * 8,), dtype=t.uint8, device="cuda",
+                                generator=g).view(t.int64)
+        self.arg = t.empty(n, dtype=t.int64, device="cuda")
+        self.wsb = self.xss.workspace_size("argsort", self.kdt, n)
+        self.ws = t.empty(max(self.wsb, 1), dtype=t.uint8, device="cuda")
+
+    def restore(self):
+        pass                         # argsort leaves its input untouched
+
+    def run(self):
+        self.xss.gpu_argsort(self.kdt, self.k0.data_ptr(), self.arg.data_ptr(), self.n,
+                             self.desc, self.desc, self.ws.data_ptr(), self.wsb,
+                             self.stream.cuda_stream)
+
+    def check(self):
+        t = self.torch
+        s = self.k0[self.arg]
+        seen = t.zeros(self.n, dtype=t.int32, device="cuda")
+        seen.index_add_(0, self.arg, t.ones(self.n, dtype=t.int32, device="cuda"))
+        if self.desc:
+            nan = t.isnan(s)
+            c = int(nan.sum())
+            r = s[c:]
+            return bool(nan[:c].all()) and bool((r[1:] <= r[:-1]).all()) and bool((seen == 1).all())
+        return bool((s[1:] >= s[:-1]).all()) and bool((seen == 1).all())
+
+    def passes(self):
+        return self.kb
+
+    def bytes_per_pass(self):        # key + index read and written (index modelled 8 B)
+        return 2 * self.n * (self.kb + self.ib)
+
+    def bytes_model(self):           # n(kb + 2P(kb+ib)) - n(ib+kb)
+        return self.n * (self.kb + 2 * self.passes() * (self.kb + self.ib)) - \
+            self.n * (self.ib + self.kb)
+
+    def host_setup(self):
+        self.hk = self.torch.empty(self.n * 8, dtype=self.torch.uint8, pin_memory=True).numpy() \
+            .view(np.dtype(self.kdt))
+        self.hk[:] = self.k0.cpu().numpy()
+
+    def host_restore(self):
+        pass
+
+    def host_run(self):
+        self.harg = self.xss.argsort(self.hk, self.desc, self.desc)
+
+    def host_bytes(self):
+        return self.n * self.kb, self.n * 8
+
+    def cpu_sample(self, m):
+        rng = np.random.default_rng(1)
+        if self.kdt == "float64":
+            x = rng.standard_normal(m)
+            u = rng.random(m)
+            x[u < 0.01] = np.nan
+            x[(u >= 0.01) & (u < 0.0125)] = 0.0
+            x[(u >= 0.0125) & (u < 0.015)] = -0.0
+            return (x,)
+        return (rng.integers(np.iinfo(np.int64).min, np.iinfo(np.int64).max, m,
+                             dtype=np.int64),)
+
+    def cpu_run(self, lib, kind, sample, threads):
+        x = sample[0]
+        arg = np.empty(x.size, np.uint64)
+        dt = 8 if self.kdt == "float64" else 7
+        if kind == "reference":
+            rc = lib.argsort(dt, x.ctypes.data, arg.ctypes.data, x.size, int(self.desc),
+                             int(self.desc))
+        else:
+            rc = lib.argsort_mt(dt, x.ctypes.data, arg.ctypes.data, x.size, int(self.desc),
+                                int(self.desc), threads)
+        assert rc == 0
+
+
+class ArgsortF64(ArgsortWorkload):
+    name = "argsort_f64"
+    kdt = "float64"
+    desc = True
+
+
+class SelectWorkload(Workload):
+    """qselect / partial_qsort of 2^27 float32 keys ~ N(0,1) (seed 2) at k."""
+
+    name = "qselect_f32"
+    dominant = None
+    partial = False
+
+    def describe(self):
+        return {"workload": f"{'partial_qsort' if self.partial else 'qselect'} float32 "
+                            f"n=2^{self.n.bit_length() - 1} N(0,1) k={self.k}",
+                "n": self.n, "k": self.k, "l2": "inputs larger than L2; restored per step"}
+
+    def setup(self):
+        t = self.torch
+        g = t.Generator(device="cuda").manual_seed(2)
+        self.k0 = t.randn(self.n, device="cuda", generator=g)
+        self.x = t.empty_like(self.k0)
+        op = "partial_qsort" if self.partial else "qselect"
+        self.wsb = self.xss.workspace_size(op, "float32", self.n, self.k)
+        self.ws = t.empty(max(self.wsb, 1), dtype=t.uint8, device="cuda")
+
+    def restore(self):
+        self.x.copy_(self.k0)
+
+    def run(self):
+        f = self.xss.gpu_partial_qsort if self.partial else self.xss.gpu_qselect
+        f("float32", self.x.data_ptr(), self.k, self.n, False, False, self.ws.data_ptr(),
+          self.wsb, self.stream.cuda_stream)
+
+    def check(self):
+        t = self.torch
+        kk = self.k - 1 if self.partial else self.k
+        kth = t.kthvalue(self.k0, kk + 1).values
+        ok = float(self.x[kk]) == float(kth)
+        ok &= bool((self.x[kk + 1:] >= self.x[kk]).all())
+        if self.partial:
+            ok &= bool(t.equal(self.x[:self.k], t.sort(self.k0).values[:self.k]))
+        return ok
+
+    def passes(self):
+        return 1
+
+    def bytes_per_pass(self):
+        return None
+
+    def bytes_model(self):           # histogram + one partition R+W (+ sort of the top k)
+        m = 3 * self.n * 4
+        if self.partial:
+            m += self.k * 4 * (1 + 2 * 4)
+        return m
+
+    def host_setup(self):
+        self.hk0 = self.k0.cpu().numpy()
+        self.hk = self.torch.empty(self.n * 4, dtype=self.torch.uint8,
+                                   pin_memory=True).numpy().view(np.float32)
+
+    def host_restore(self):
+        np.copyto(self.hk, self.hk0)
+
+    def host_run(self):
+        (self.xss.partial_qsort if self.partial else self.xss.qselect)(self.hk, self.k)
+
+    def host_bytes(self):
+        return self.n * 4, self.n * 4
+
+    def cpu_sample(self, m):
+        return (np.random.default_rng(2).standard_normal(m).astype(np.float32),)
+
+    def cpu_run(self, lib, kind, sample, threads):
+        x = sample[0].copy()
+        kk = min(self.k, x.size - 1) * x.size // self.n if self.k > 1000 else min(self.k, x.size - 1)
+        f = lib.partial_qsort if self.partial else lib.qselect
+        assert f(5, x.ctypes.data, max(kk, 1) if self.partial else kk, x.size, 0, 0) == 0
+
+
+class PartialWorkload(SelectWorkload):
+    name = "partial_f32"
+    partial = True
+
+
 SEG_LITERAL = -1
+DTYPE_OF = {"keyvalue_qsort": "int64", "qsort_f32": "f32", "segmented": "int32",
+            "qsort_f32_2e20": "f32", "argsort_i64": "int64", "argsort_f64": "f64",
+            "qselect_f32": "f32", "partial_f32": "f32"}
 WORKLOADS = {"keyvalue_qsort": (KeyValueSort, 1 << 28), "qsort_f32": (QsortF32, 1 << 28),
-             "segmented": (SegmentedSort, SEG_LITERAL)}
+             "segmented": (SegmentedSort, SEG_LITERAL),
+             "qsort_f32_2e20": (QsortF32Small, 1 << 20),
+             "argsort_i64": (ArgsortWorkload, 1 << 28), "argsort_f64": (ArgsortF64, 1 << 28),
+             "qselect_f32": (SelectWorkload, 1 << 27), "partial_f32": (PartialWorkload, 1 << 27)}
 
 
 # ---------------------------------------------------------------------------
@@ -435,8 +640,7 @@ def reference_arm(args):
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": dt / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None,
-            "dtype": {"keyvalue_qsort": "int64", "qsort_f32": "f32",
-                      "segmented": "int32"}[args.workload],
+            "dtype": DTYPE_OF[args.workload],
             "data": "synthetic",
             "config": {"workload": f"{args.workload} (bounded CPU sample of {m} keys)",
                        "full_n": n_full},
@@ -612,6 +816,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--workload", default="keyvalue_qsort",
                     choices=sorted(WORKLOADS) + ["serving"])
+    ap.add_argument("--k", type=int, default=1 << 26, help="select workloads: k")
     ap.add_argument("--rate", type=float, default=20000.0, help="serving: offered req/s")
     ap.add_argument("--duration", type=float, default=2.0, help="serving: seconds of arrivals")
     ap.add_argument("--ring-gb", type=int, default=16, help="serving: pinned output ring")
@@ -650,6 +855,11 @@ def main():
     stream = torch.cuda.Stream()
     wl = cls(torch, xss, n, stream)
     n = wl.n
+    if hasattr(wl, "partial"):
+        wl.k = args.k
+    flush = None
+    if getattr(wl, "flush_l2", False):
+        flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
     with torch.cuda.stream(stream):
         wl.setup()
     torch.cuda.synchronize()
@@ -675,6 +885,8 @@ def main():
     for _ in range(args.steps):
         with torch.cuda.stream(stream):
             wl.restore()
+            if flush is not None:
+                flush.zero_()        # evict the input from L2 (untimed)
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
         with torch.cuda.stream(stream):
@@ -686,7 +898,7 @@ def main():
     wall = time.perf_counter() - t_wall
     clk = clocks.stop()
     launches = xss.prof_launches() - launches0
-    dom_ms, dom_launches = xss.prof_read(wl.dominant)
+    dom_ms, dom_launches = xss.prof_read(wl.dominant) if wl.dominant else (0.0, 0)
     dom_steps = args.steps
     if dom_launches == 0 and hasattr(wl, "run_nograph"):
         # kernels inside a replayed graph cannot be bracketed by events: time
@@ -730,6 +942,13 @@ def main():
     active = dom_launches / dom_steps if dom_launches else 0
     avg_pass_ms = dom_ms / dom_launches if dom_launches else float("nan")
     achieved = wl.bytes_per_pass() / (avg_pass_ms / 1e3) / 1e9 if dom_launches else None
+    kernel_name = "onesweep radix pass"
+    if wl.dominant is None:
+        # select: several short kernels; the roofline covers the whole operation
+        kernel_name = "select (all kernels of one call)"
+        avg_pass_ms = ms_per_step
+        achieved = wl.bytes_model() / (ms_per_step / 1e3) / 1e9
+        active = launches / args.steps
     traffic = _traffic(args.workload)
 
     e2e = None
@@ -757,11 +976,10 @@ def main():
             "metric": "Gkeys/s", "value": value, "unit": "Gkeys/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": {"keyvalue_qsort": "int64", "qsort_f32": "f32",
-                      "segmented": "int32"}[args.workload],
+            "dtype": DTYPE_OF[args.workload],
             "data": "synthetic (seeded, generated on device)",
             "config": {**wl.describe(), "parallelism": f"replicas x{world}"},
-            "roofline": {"bound": "hbm", "kernel": "onesweep radix pass",
+            "roofline": {"bound": "hbm", "kernel": kernel_name,
                          "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": (achieved / peak) if achieved else None,
                          "peak_source": peak_src,

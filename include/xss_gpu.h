@@ -89,9 +89,9 @@ int xss_gpu_selftest_bounded_wait(int which, unsigned spin_limit, xss_stream_t s
 
 /* ------------------------------------------------------------------ */
 /* Device-pointer entry points.  Arrays live in device memory; work is   */
-/* enqueued on `stream`; the status of bounded waits is checked with a  */
-/* small device->host read at the end of the call (the call syncs the   */
-/* stream only for that read).                                          */
+/* enqueued on `stream` and the call returns without synchronising      */
+/* (except when the cached workspace grows).  A bounded wait that gave  */
+/* up is reported later by xss_gpu_stream_status.                       */
 /* ------------------------------------------------------------------ */
 
 /* x86simdsort::qsort (lib/x86simdsort.h:15-18) */
