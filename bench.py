@@ -898,6 +898,12 @@ def main():
     wall = time.perf_counter() - t_wall
     clk = clocks.stop()
     launches = xss.prof_launches() - launches0
+    # event-timed device time per kernel kind (per step), the breakdown behind ms_per_step
+    kernels = {}
+    for kind in xss.PROF_KINDS:
+        k_ms, k_n = xss.prof_read(kind)
+        if k_n:
+            kernels[kind] = {"ms_per_step": k_ms / args.steps, "launches_per_step": k_n / args.steps}
     dom_ms, dom_launches = xss.prof_read(wl.dominant) if wl.dominant else (0.0, 0)
     dom_steps = args.steps
     if dom_launches == 0 and hasattr(wl, "run_nograph"):
@@ -991,6 +997,7 @@ def main():
             "e2e": e2e,
             "cpu_baseline": cpu,
             "gpu_launches": launches,
+            "kernels": kernels,
             "clocks": clk,
             "checked": checked,
             **({"percall_ms": percall, "speedup_vs_percall": percall / ms_per_step}

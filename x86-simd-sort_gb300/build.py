@@ -44,7 +44,8 @@ def build(force: bool = False, verbose_ptxas: bool = False) -> str:
     os.makedirs(BUILD, exist_ok=True)
     cu = sorted(glob.glob(os.path.join(CSRC, "*.cu")))
     cpp = sorted(glob.glob(os.path.join(CSRC, "*.cpp")))
-    headers = glob.glob(os.path.join(CSRC, "*.cuh")) + glob.glob(os.path.join(INCLUDE, "*.h"))
+    headers = glob.glob(os.path.join(CSRC, "*.cuh")) + glob.glob(os.path.join(CSRC, "*.h")) + \
+        glob.glob(os.path.join(INCLUDE, "*.h"))
     hdr_time = _newest(headers)
     jobs = []
     objs = []

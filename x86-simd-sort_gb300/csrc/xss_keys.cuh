@@ -121,3 +121,32 @@ __device__ __forceinline__ void st_relaxed_u32(uint32_t *p, uint32_t v)
 {
     asm volatile("st.relaxed.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
+
+// N consecutive status words (N = 1, 2, 4; p aligned to 4N bytes).  Each
+// 32-bit element is read / written as one relaxed access of its own.
+template <int N> __device__ __forceinline__ void ld_relaxed_vec(const uint32_t *p, uint32_t (&v)[N])
+{
+    static_assert(N == 1 || N == 2 || N == 4, "1, 2 or 4 words");
+    if constexpr (N == 1) {
+        v[0] = ld_relaxed_u32(p);
+    } else if constexpr (N == 2) {
+        asm volatile("ld.relaxed.gpu.global.v2.u32 {%0, %1}, [%2];"
+                     : "=r"(v[0]), "=r"(v[1]) : "l"(p) : "memory");
+    } else {
+        asm volatile("ld.relaxed.gpu.global.v4.u32 {%0, %1, %2, %3}, [%4];"
+                     : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]) : "l"(p) : "memory");
+    }
+}
+template <int N> __device__ __forceinline__ void st_relaxed_vec(uint32_t *p, const uint32_t (&v)[N])
+{
+    static_assert(N == 1 || N == 2 || N == 4, "1, 2 or 4 words");
+    if constexpr (N == 1) {
+        st_relaxed_u32(p, v[0]);
+    } else if constexpr (N == 2) {
+        asm volatile("st.relaxed.gpu.global.v2.u32 [%0], {%1, %2};"
+                     ::"l"(p), "r"(v[0]), "r"(v[1]) : "memory");
+    } else {
+        asm volatile("st.relaxed.gpu.global.v4.u32 [%0], {%1, %2, %3, %4};"
+                     ::"l"(p), "r"(v[0]), "r"(v[1]), "r"(v[2]), "r"(v[3]) : "memory");
+    }
+}

@@ -59,13 +59,20 @@ __device__ __forceinline__ void *pick3(void *const (&b)[3], int i)
 //   MINB:         CTAs per SM the register budget is cut for
 //   LB:           predecessors probed per look-back round trip
 //   RANK:         1 = peer masks from eight ballots, 0 = from shared atomicOr
-//   PERSIST:      1 = resident CTAs with TMA prefetch, 0 = one CTA per tile
+//   PERSIST:      0 = one CTA per tile, 1 = resident CTAs with TMA prefetch,
+//                 2 = resident CTAs with ordinary loads (one staging buffer)
+//   DPT:          look-back placement.  0: after ranking, one digit per
+//                 thread; 1, 2, 4: right after the counts, by 256 / DPT
+//                 threads with DPT digits each while the other warps rank
 // Each line can be overridden at build time (a pre-included header defining
-// XSS_CFG_K32 etc.) for tuning.  Defaults are the fastest measured on GB300
-// (2^28 keys, uniform): keys-only 32-bit 4.95 ms/sort, int64->uint64 21.7 ms.
-template <int B, int I, int M, int L, int R, int P> struct CfgT {
-    static constexpr int BLOCK = B, ITEMS = I, MINB = M, LB = L, RANK = R, PERSIST = P;
+// XSS_CFG_K32 etc.) for tuning; xss_tuning.h, written by autotune.py, holds
+// the lines it measured fastest and takes precedence over the defaults below.
+template <int B, int I, int M, int L, int R, int P, int D = 0> struct CfgT {
+    static constexpr int BLOCK = B, ITEMS = I, MINB = M, LB = L, RANK = R, PERSIST = P, DPT = D;
 };
+#if __has_include("xss_tuning.h")
+#include "xss_tuning.h"
+#endif
 #ifndef XSS_CFG_DEFAULT
 #define XSS_CFG_DEFAULT 256, 12, 2, 16, 1, 0
 #endif
@@ -73,7 +80,7 @@ template <int B, int I, int M, int L, int R, int P> struct CfgT {
 #define XSS_CFG_K16 512, 16, 2, 16, 0, 1
 #endif
 #ifndef XSS_CFG_K32
-#define XSS_CFG_K32 512, 16, 2, 16, 0, 1
+#define XSS_CFG_K32 512, 16, 2, 16, 0, 1, 1
 #endif
 #ifndef XSS_CFG_K64
 #define XSS_CFG_K64 256, 16, 2, 16, 1, 1
@@ -82,7 +89,7 @@ template <int B, int I, int M, int L, int R, int P> struct CfgT {
 #define XSS_CFG_K32V32 512, 10, 2, 16, 1, 0
 #endif
 #ifndef XSS_CFG_K64V64
-#define XSS_CFG_K64V64 256, 12, 2, 16, 1, 0
+#define XSS_CFG_K64V64 512, 6, 2, 16, 1, 0, 1
 #endif
 template <typename C, typename V> struct PassCfg : CfgT<XSS_CFG_DEFAULT> {};
 template <> struct PassCfg<uint16_t, NoVal> : CfgT<XSS_CFG_K16> {};
@@ -96,57 +103,76 @@ template <typename C, typename V> constexpr size_t pass_tile_size()
     return (size_t)PassCfg<C, V>::BLOCK * PassCfg<C, V>::ITEMS;
 }
 
-// Exclusive prefix of digit d over tiles [0, tile) by decoupled look-back:
-// probe LB predecessors per round trip, add aggregates until the first
-// inclusive prefix; an entry not yet published is probed again (bounded).
+// Exclusive prefixes of DPT consecutive digits d0.. over tiles [first, tile)
+// by decoupled look-back: probe LB predecessors per round trip (one vector
+// load of DPT status words each), add aggregates until each digit meets its
+// first inclusive prefix; a row with an unpublished word of a digit still
+// walking is probed again (bounded).
 #ifndef XSS_LOOKBACK_FIRST
 #define XSS_LOOKBACK_FIRST 16
 #endif
-template <int LB>
-__device__ __forceinline__ uint32_t lookback_excl(const uint32_t *st_pass, uint32_t tile,
-                                                  uint32_t first, int d, unsigned *err,
-                                                  uint32_t spin_limit = XSS_SPIN_LIMIT)
+template <int LB, int DPT>
+__device__ __forceinline__ void lookback_excl(const uint32_t *st_pass, uint32_t tile,
+                                              uint32_t first, int d0, unsigned *err,
+                                              uint32_t (&excl)[DPT],
+                                              uint32_t spin_limit = XSS_SPIN_LIMIT)
 {
-    uint32_t excl = 0;
+#pragma unroll
+    for (int j = 0; j < DPT; ++j) excl[j] = 0;
+    uint32_t pending = (1u << DPT) - 1u;   // digits still walking
     int p = (int)tile - 1;
     const int lo = (int)first;
     uint32_t spins = 0;
     // the first round probes only the nearest predecessors; later rounds LB
     int width = XSS_LOOKBACK_FIRST < LB ? XSS_LOOKBACK_FIRST : LB;
     while (p >= lo) {
-        uint32_t v[LB];
-#pragma unroll
-        for (int w = 0; w < LB; ++w)
-            v[w] = (w < width && p - w >= lo)
-                       ? ld_relaxed_u32(st_pass + (size_t)(p - w) * RADIX + d)
-                       : (p - w >= lo ? 0u : FLAG_PRE);
-        int used = 0;
-        bool done = false;
+        uint32_t v[LB][DPT];
 #pragma unroll
         for (int w = 0; w < LB; ++w) {
-            if (done || used != w) break;
-            const uint32_t f = v[w] & FLAG_MASK;
-            if (f == 0u) break;
-            excl += v[w] & COUNT_MASK;
-            ++used;
-            if (f == FLAG_PRE) done = true;
+            if (w < width && p - w >= lo) {
+                ld_relaxed_vec<DPT>(st_pass + (size_t)(p - w) * RADIX + d0, v[w]);
+            } else {
+#pragma unroll
+                for (int j = 0; j < DPT; ++j) v[w][j] = p - w >= lo ? 0u : FLAG_PRE;
+            }
         }
-        if (done) return excl;
+        int used = 0;
+#pragma unroll
+        for (int w = 0; w < LB; ++w) {
+            if (pending == 0u || used != w) break;
+            bool ready = true;
+#pragma unroll
+            for (int j = 0; j < DPT; ++j)
+                if (((pending >> j) & 1u) && (v[w][j] & FLAG_MASK) == 0u) ready = false;
+            if (!ready) break;
+#pragma unroll
+            for (int j = 0; j < DPT; ++j) {
+                if ((pending >> j) & 1u) {
+                    excl[j] += v[w][j] & COUNT_MASK;
+                    if ((v[w][j] & FLAG_MASK) == FLAG_PRE) pending &= ~(1u << j);
+                }
+            }
+            ++used;
+        }
+        if (pending == 0u) return;
         if (used == 0 && ++spins > spin_limit) {
             atomicOr(err, XSS_DEVERR_TIMEOUT);
-            return excl;
+            return;
         }
         p -= used;
         width = LB;
     }
-    return excl;
 }
 
 // Shared-memory scratch of the per-tile body (static part).
 template <int BLOCK> struct PassSmem {
-    uint32_t whist[(BLOCK / 32) * RADIX];  // per-warp digit counts, then running offsets
-    uint32_t match[(BLOCK / 32) * RADIX];  // per-warp lane masks (kept zero between items)
+    // Per-warp words per digit: the first half holds 32-bit digit counts,
+    // then running offsets; the second half (RANK 0) lane masks.  Zero
+    // between tiles.
+    unsigned long long wm[(BLOCK / 32) * RADIX];
     int32_t off[RADIX];                     // global offset - local start, per digit
+    uint32_t cnt[RADIX];                    // tile count per digit
+    uint32_t lstart[RADIX];                 // tile-local start per digit
     uint32_t scan[BLOCK / 32];
 };
 
@@ -167,9 +193,9 @@ struct TileJob {
 // thread reads any more once the first barrier here is passed.
 // after_rank() runs on every thread once the tile is staged (the persistent
 // form claims and prefetches its next tile there).
-// Pre: ps.whist is zero.  Post: zero again after the caller's next barrier.
-template <typename C, typename V, int BLOCK, int ITEMS, int LB, int RANK, typename VS,
-          typename AfterRank>
+// Pre: ps.wm is zero.  Post: zero again after the caller's next barrier.
+template <typename C, typename V, int BLOCK, int ITEMS, int LB, int RANK, int DPT,
+          typename VS, typename AfterRank>
 __device__ __forceinline__ void pass_tile(const RadixArgs &a, const PassDesc &pd, int pass,
                                           const TileJob &job, const C (&key)[ITEMS],
                                           const VS (&val)[ITEMS], C *s_k, VS *s_v,
@@ -184,7 +210,8 @@ __device__ __forceinline__ void pass_tile(const RadixArgs &a, const PassDesc &pd
     const uint32_t tile = job.tile;
     const int shift = pass * RADIX_BITS;
     const uint32_t tile_base = job.base;
-    uint32_t *wh = ps.whist + warp * RADIX;
+    uint32_t *const hist32 = reinterpret_cast<uint32_t *>(ps.wm);
+    uint32_t *wh = hist32 + warp * RADIX;
 
     // ---- per-warp digit counts (independent shared atomics)
 #pragma unroll
@@ -197,7 +224,7 @@ __device__ __forceinline__ void pass_tile(const RadixArgs &a, const PassDesc &pd
     uint32_t cnt = 0;
     if (tid < RADIX) {
 #pragma unroll
-        for (int w = 0; w < WARPS; ++w) cnt += ps.whist[w * RADIX + tid];
+        for (int w = 0; w < WARPS; ++w) cnt += hist32[w * RADIX + tid];
         st_relaxed_u32(st_tile + tid, (tile == job.first ? FLAG_PRE : FLAG_AGG) | cnt);
     }
     uint32_t total;
@@ -206,12 +233,38 @@ __device__ __forceinline__ void pass_tile(const RadixArgs &a, const PassDesc &pd
         uint32_t run = local_start;
 #pragma unroll
         for (int w = 0; w < WARPS; ++w) {
-            const uint32_t c = ps.whist[w * RADIX + tid];
-            ps.whist[w * RADIX + tid] = run;
+            const uint32_t c = hist32[w * RADIX + tid];
+            hist32[w * RADIX + tid] = run;
             run += c;
         }
+        ps.cnt[tid] = cnt;
+        ps.lstart[tid] = local_start;
     }
     __syncthreads();
+
+    // ---- look-back for this tile's global offsets.  DPT > 0: as soon as the
+    // counts are out, RADIX / DPT threads (the first warps) walk back, DPT
+    // digits each, while the other warps already rank; the walkers rank
+    // afterwards.  DPT 0: after ranking, one digit per thread.
+    static_assert(DPT == 0 || DPT == 1 || DPT == 2 || DPT == 4, "look-back placement");
+    constexpr int DW = DPT == 0 ? 1 : DPT;   // digits per walking thread
+    auto walk = [&]() {
+        const int d0 = tid * DW;
+        uint32_t excl[DW];
+#pragma unroll
+        for (int j = 0; j < DW; ++j) excl[j] = 0;
+        if (tile > job.first) {
+            lookback_excl<LB, DW>(job.st_pass, tile, job.first, d0, a.err, excl);
+            uint32_t pre[DW];
+#pragma unroll
+            for (int j = 0; j < DW; ++j) pre[j] = FLAG_PRE | ((excl[j] + ps.cnt[d0 + j]) & COUNT_MASK);
+            st_relaxed_vec<DW>(st_tile + d0, pre);
+        }
+#pragma unroll
+        for (int j = 0; j < DW; ++j)
+            ps.off[d0 + j] = (int32_t)(job.start[d0 + j] + excl[j]) - (int32_t)ps.lstart[d0 + j];
+    };
+    if (DPT != 0 && tid < RADIX / DW) walk();
 
     // ---- stable rank (digit, warp, item, lane) and stage in digit order.
     // The lanes sharing a digit find each other either by eight ballots, one
@@ -221,7 +274,7 @@ __device__ __forceinline__ void pass_tile(const RadixArgs &a, const PassDesc &pd
     // The highest such lane advances the warp's running offset for the digit.
     {
         const uint32_t lt_mask = (1u << lane) - 1u;
-        uint32_t *mt = ps.match + warp * RADIX;
+        uint32_t *mt = hist32 + (WARPS + warp) * RADIX;   // RANK 0 only
 #pragma unroll
         for (int j = 0; j < ITEMS; ++j) {
             const uint32_t d = uint32_t(key[j] >> shift) & (RADIX - 1);
@@ -254,16 +307,7 @@ __device__ __forceinline__ void pass_tile(const RadixArgs &a, const PassDesc &pd
         }
     }
     after_rank();
-
-    // ---- look-back for this tile's global offsets
-    if (tid < RADIX) {
-        uint32_t excl = 0;
-        if (tile > job.first) {
-            excl = lookback_excl<LB>(job.st_pass, tile, job.first, tid, a.err);
-            st_relaxed_u32(st_tile + tid, FLAG_PRE | ((excl + cnt) & COUNT_MASK));
-        }
-        ps.off[tid] = (int32_t)(job.start[tid] + excl) - (int32_t)local_start;
-    }
+    if (DPT == 0 && tid < RADIX) walk();
     __syncthreads();
 
     // ---- scatter runs of equal digits to consecutive global addresses
@@ -286,7 +330,7 @@ __device__ __forceinline__ void pass_tile(const RadixArgs &a, const PassDesc &pd
             }
         }
     }
-    for (int i = tid; i < WARPS * RADIX; i += BLOCK) ps.whist[i] = 0;
+    for (int i = tid; i < WARPS * RADIX; i += BLOCK) ps.wm[i] = 0;
 }
 
 struct NoAfterRank {
@@ -296,7 +340,7 @@ struct NoAfterRank {
 // ---------------------------------------------------------------------------
 // One CTA per tile; the tile id comes from an in-order atomic counter, so a
 // tile only waits on tiles whose CTAs are already running.
-template <typename C, typename V, int BLOCK, int ITEMS, int MINB, int LB, int RANK>
+template <typename C, typename V, int BLOCK, int ITEMS, int MINB, int LB, int RANK, int DPT>
 __global__ void __launch_bounds__(BLOCK, MINB) onesweep_kernel(RadixArgs a, int pass)
 {
     constexpr int TILE = BLOCK * ITEMS;
@@ -313,10 +357,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) onesweep_kernel(RadixArgs a, int 
     VS *s_v = reinterpret_cast<VS *>(s_dyn + TILE * sizeof(C));
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    for (int i = tid; i < (BLOCK / 32) * RADIX; i += BLOCK) {
-        ps.whist[i] = 0;
-        ps.match[i] = 0;
-    }
+    for (int i = tid; i < (BLOCK / 32) * RADIX; i += BLOCK) ps.wm[i] = 0;
     if (tid == 0) s_tile = atomicAdd(&a.hdr->tile_ctr[pass], 1u);
     __syncthreads();
     const uint32_t tile = s_tile;
@@ -347,21 +388,24 @@ __global__ void __launch_bounds__(BLOCK, MINB) onesweep_kernel(RadixArgs a, int 
     }
     const TileJob job{tile, 0u, tile * (uint32_t)TILE, n, a.hdr->start[pass],
                       a.status + (size_t)pass * a.num_tiles * RADIX};
-    pass_tile<C, V, BLOCK, ITEMS, LB, RANK>(a, pd, pass, job, key, val, s_k, s_v, ps,
+    pass_tile<C, V, BLOCK, ITEMS, LB, RANK, DPT>(a, pd, pass, job, key, val, s_k, s_v, ps,
                                       static_cast<C *>(pick3(a.kbuf, pd.dst)), vdst,
                                       NoAfterRank{});
 }
 
 // ---------------------------------------------------------------------------
 // Resident CTAs that keep claiming tiles from the same in-order counter.
-// Once a tile is ranked and staged, the CTA claims its next tile and starts
-// its bulk copy (TMA) into the other buffer, so the load overlaps the current
-// tile's look-back and scatter.  Claims are in increasing order per CTA,
+// Once a tile is ranked and staged, the CTA claims its next tile and (PF)
+// starts its bulk copy (TMA) into the other buffer, so the load overlaps the
+// current tile's scatter.  Without PF the CTA keeps one staging buffer and
+// reads each tile with ordinary loads: less shared memory per CTA, more CTAs
+// per SM, and no per-tile CTA launch.  Claims are in increasing order per CTA,
 // which keeps the look-back free of deadlock: the lowest unfinished tile is
 // always the current tile of the CTA holding it, and every tile below it is
 // finished.  Partial tiles and sources that are not 16-byte aligned are read
 // with ordinary loads.
-template <typename C, typename V, int BLOCK, int ITEMS, int MINB, int LB, int RANK>
+template <typename C, typename V, int BLOCK, int ITEMS, int MINB, int LB, int RANK, int DPT,
+          bool PF>
 __global__ void __launch_bounds__(BLOCK, MINB) onesweep_persist_kernel(RadixArgs a, int pass)
 {
     constexpr int TILE = BLOCK * ITEMS;
@@ -377,8 +421,9 @@ __global__ void __launch_bounds__(BLOCK, MINB) onesweep_persist_kernel(RadixArgs
     __shared__ uint32_t s_tile[2];
     __shared__ __align__(8) uint64_t s_bar[2];
     extern __shared__ __align__(128) unsigned char s_dyn[];
+    constexpr int NBUF = PF ? 2 : 1;
     C *const s_k0 = reinterpret_cast<C *>(s_dyn);
-    VS *const s_v0 = reinterpret_cast<VS *>(s_dyn + 2 * TILE * sizeof(C));
+    VS *const s_v0 = reinterpret_cast<VS *>(s_dyn + NBUF * TILE * sizeof(C));
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const uint32_t n = (uint32_t)a.n;
@@ -392,7 +437,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) onesweep_persist_kernel(RadixArgs
         vdst = static_cast<V *>(pick3(a.vbuf, pd.vdst));
     }
     const bool load_vals = HAS_V && !pd.gen_idx;
-    const bool tma = (reinterpret_cast<uintptr_t>(ksrc) & 15) == 0 &&
+    const bool tma = PF && (reinterpret_cast<uintptr_t>(ksrc) & 15) == 0 &&
                      (!load_vals || (reinterpret_cast<uintptr_t>(vsrc) & 15) == 0);
     const uint32_t tile_bytes = TILE * (uint32_t)(sizeof(C) + (load_vals ? VSZ : 0));
 
@@ -405,10 +450,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) onesweep_persist_kernel(RadixArgs
     };
     auto by_tma = [&](uint32_t t) { return tma && t < num_tiles && (size_t)t * TILE + TILE <= n; };
 
-    for (int i = tid; i < (BLOCK / 32) * RADIX; i += BLOCK) {
-        ps.whist[i] = 0;
-        ps.match[i] = 0;
-    }
+    for (int i = tid; i < (BLOCK / 32) * RADIX; i += BLOCK) ps.wm[i] = 0;
     if (tid == 0) {
         mbar_init(&s_bar[0], 1);
         mbar_init(&s_bar[1], 1);
@@ -426,8 +468,8 @@ __global__ void __launch_bounds__(BLOCK, MINB) onesweep_persist_kernel(RadixArgs
         if (tile >= num_tiles) break;
         const uint32_t tile_base = tile * (uint32_t)TILE;
         const uint32_t local0 = (uint32_t)warp * (ITEMS * 32) + lane;
-        C *s_k = s_k0 + cur * TILE;
-        VS *s_v = s_v0 + cur * TILE;
+        C *s_k = s_k0 + (PF ? cur : 0) * TILE;
+        VS *s_v = s_v0 + (PF ? cur : 0) * TILE;
         C key[ITEMS];
         VS val[ITEMS];
         if (by_tma(tile)) {
@@ -477,7 +519,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) onesweep_persist_kernel(RadixArgs
         };
         const TileJob job{tile, 0u, tile_base, n, a.hdr->start[pass],
                           a.status + (size_t)pass * num_tiles * RADIX};
-        pass_tile<C, V, BLOCK, ITEMS, LB, RANK>(a, pd, pass, job, key, val, s_k, s_v, ps, kdst, vdst,
+        pass_tile<C, V, BLOCK, ITEMS, LB, RANK, DPT>(a, pd, pass, job, key, val, s_k, s_v, ps, kdst, vdst,
                                           claim_next);
         __syncthreads();
     }

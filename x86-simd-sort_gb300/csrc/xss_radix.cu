@@ -24,17 +24,24 @@ namespace xss {
 // fused with clearing the look-back status words.  The last CTA to finish
 // turns the histograms into per-pass bucket starts and writes the pass plan:
 // a pass whose digit is the same for every key is skipped.
+// Lanes count into four copies of the histograms (lane & 3), so a digit that
+// most keys share (the top byte of floats, small-range integers) costs at
+// most an 8-way same-address conflict instead of 32-way; the copies sit 8
+// banks apart.
+constexpr int HIST_COPIES = 4;
+constexpr int HIST_COPY_STRIDE = MAX_PASSES * RADIX + 8;
 template <typename C>
 __global__ void __launch_bounds__(256) hist_kernel(RadixArgs a)
 {
-    __shared__ uint32_t sh[MAX_PASSES * RADIX];
+    __shared__ uint32_t sh_all[HIST_COPIES * HIST_COPY_STRIDE];
     __shared__ uint32_t s_scan[8];
     __shared__ int s_last;
     __shared__ int s_active[MAX_PASSES];
     const int tid = threadIdx.x;
     const int P = a.passes;
-    for (int i = tid; i < P * RADIX; i += 256) sh[i] = 0;
+    for (int i = tid; i < HIST_COPIES * HIST_COPY_STRIDE; i += 256) sh_all[i] = 0;
     __syncthreads();
+    uint32_t *const sh = sh_all + (tid & (HIST_COPIES - 1)) * HIST_COPY_STRIDE;
 
     const C *src = static_cast<const C *>(a.kbuf[0]);
     const size_t n = a.n;
@@ -66,8 +73,12 @@ __global__ void __launch_bounds__(256) hist_kernel(RadixArgs a)
     for (size_t i = gtid; i < nst4; i += stride) st4[i] = make_uint4(0, 0, 0, 0);
 
     __syncthreads();
-    for (int i = tid; i < P * RADIX; i += 256)
-        if (sh[i]) atomicAdd(&a.hdr->hist[0][0] + i, sh[i]);
+    for (int i = tid; i < P * RADIX; i += 256) {
+        uint32_t t = 0;
+#pragma unroll
+        for (int c = 0; c < HIST_COPIES; ++c) t += sh_all[c * HIST_COPY_STRIDE + i];
+        if (t) atomicAdd(&a.hdr->hist[0][0] + i, t);
+    }
     __threadfence();
     __syncthreads();
     if (tid == 0) s_last = (atomicAdd(&a.hdr->done_ctr, 1u) == gridDim.x - 1);
@@ -225,17 +236,44 @@ static int small_sort_launch(int op, KeyXform xf, void *keys, void *vals,
 }
 
 // Pass-kernel form: the tuned choice of PassCfg (PERSIST), unless the
-// environment forces one: XSS_ONESWEEP=tile (one CTA per tile) or
-// XSS_ONESWEEP=persist (resident CTAs with TMA prefetch).
-static bool use_persistent_pass(bool tuned)
+// environment forces one: XSS_ONESWEEP=tile (one CTA per tile),
+// XSS_ONESWEEP=persist (resident CTAs with TMA prefetch) or
+// XSS_ONESWEEP=resident (resident CTAs, ordinary loads).
+static int pass_form(int tuned)
 {
     static const int forced = [] {
         const char *e = getenv("XSS_ONESWEEP");
         if (e && strcmp(e, "tile") == 0) return 0;
         if (e && strcmp(e, "persist") == 0) return 1;
+        if (e && strcmp(e, "resident") == 0) return 2;
         return -1;
     }();
-    return forced < 0 ? tuned : forced == 1;
+    return forced < 0 ? tuned : forced;
+}
+
+// Launch every active pass with resident CTAs (grid = what fits on the SMs).
+template <typename C, typename V, int BLOCK, int ITEMS, int MINB, int LB, int RANK, int DPT,
+          bool PF>
+static int resident_passes(const RadixArgs &a, int sms, cudaStream_t s, const LaunchOpts &o)
+{
+    constexpr size_t TILE = (size_t)BLOCK * ITEMS;
+    constexpr bool HAS_V = !std::is_same<V, NoVal>::value;
+    const size_t smem = (PF ? 2 : 1) * TILE * (sizeof(C) + (HAS_V ? sizeof(V) : 0));
+    auto kern = onesweep_persist_kernel<C, V, BLOCK, ITEMS, MINB, LB, RANK, DPT, PF>;
+    static int per_sm = 0;
+    if (!per_sm) {
+        XSS_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)smem));
+        int v = 0;
+        XSS_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, kern, BLOCK, smem));
+        per_sm = std::max(v, 1);
+    }
+    const uint32_t grid = (uint32_t)std::min<size_t>(a.num_tiles, (size_t)per_sm * sms);
+    for (int p = 0; p < a.passes; ++p) {
+        XSS_LAUNCH_OPT(o, PK_ONESWEEP, s, kern<<<grid, BLOCK, smem, s>>>(a, p));
+        XSS_CUDA_TRY(cudaGetLastError());
+    }
+    return XSS_OK;
 }
 
 template <typename C, typename V>
@@ -245,7 +283,7 @@ static int onesweep_launch(int op, KeyXform xf, void *keys, void *vals, uint64_t
 {
     using Cfg = PassCfg<C, V>;
     constexpr int BLOCK = Cfg::BLOCK, ITEMS = Cfg::ITEMS, MINB = Cfg::MINB, LB = Cfg::LB,
-                  RANK = Cfg::RANK;
+                  RANK = Cfg::RANK, DPT = Cfg::DPT;
     constexpr size_t TILE = (size_t)BLOCK * ITEMS;
     constexpr bool HAS_V = !std::is_same<V, NoVal>::value;
     const int kbytes = sizeof(C);
@@ -280,25 +318,15 @@ static int onesweep_launch(int op, KeyXform xf, void *keys, void *vals, uint64_t
     XSS_CUDA_TRY(cudaGetLastError());
 
     const size_t vsz = HAS_V ? sizeof(V) : 0;
-    if (use_persistent_pass(Cfg::PERSIST != 0)) {
-        const size_t smem = 2 * TILE * (sizeof(C) + vsz);
-        auto kern = onesweep_persist_kernel<C, V, BLOCK, ITEMS, MINB, LB, RANK>;
-        static int per_sm = 0;
-        if (!per_sm) {
-            XSS_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                              (int)smem));
-            int v = 0;
-            XSS_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, kern, BLOCK, smem));
-            per_sm = std::max(v, 1);
-        }
-        const uint32_t grid = (uint32_t)std::min<size_t>(a.num_tiles, (size_t)per_sm * sms);
-        for (int p = 0; p < a.passes; ++p) {
-            XSS_LAUNCH_OPT(o, PK_ONESWEEP, s, kern<<<grid, BLOCK, smem, s>>>(a, p));
-            XSS_CUDA_TRY(cudaGetLastError());
-        }
+    const int form = pass_form(Cfg::PERSIST);
+    if (form != 0) {
+        const int rc = form == 1
+            ? resident_passes<C, V, BLOCK, ITEMS, MINB, LB, RANK, DPT, true>(a, sms, s, o)
+            : resident_passes<C, V, BLOCK, ITEMS, MINB, LB, RANK, DPT, false>(a, sms, s, o);
+        if (rc) return rc;
     } else {
         const size_t smem = TILE * (sizeof(C) + vsz);
-        auto kern = onesweep_kernel<C, V, BLOCK, ITEMS, MINB, LB, RANK>;
+        auto kern = onesweep_kernel<C, V, BLOCK, ITEMS, MINB, LB, RANK, DPT>;
         static bool attr_set = false;
         if (!attr_set) {
             XSS_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,

@@ -152,7 +152,7 @@ __global__ void __launch_bounds__(256) seg_scan_kernel(SegArgs a)
 }
 
 // ---- large segments: one LSD pass over every large segment's tiles ----------
-template <typename C, typename V, int BLOCK, int ITEMS, int LB, int RANK>
+template <typename C, typename V, int BLOCK, int ITEMS, int LB, int RANK, int DPT>
 __global__ void __launch_bounds__(BLOCK, 2) seg_pass_kernel(SegArgs a, int pass)
 {
     constexpr int TILE = BLOCK * ITEMS;
@@ -164,10 +164,7 @@ __global__ void __launch_bounds__(BLOCK, 2) seg_pass_kernel(SegArgs a, int pass)
     C *s_k = reinterpret_cast<C *>(s_dyn);
     VS *s_v = reinterpret_cast<VS *>(s_dyn + TILE * sizeof(C));
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    for (int i = tid; i < (BLOCK / 32) * RADIX; i += BLOCK) {
-        ps.whist[i] = 0;
-        ps.match[i] = 0;
-    }
+    for (int i = tid; i < (BLOCK / 32) * RADIX; i += BLOCK) ps.wm[i] = 0;
     if (tid == 0) s_tile = atomicAdd(&a.tile_ctr[pass], 1u);
     __syncthreads();
     const uint32_t t = s_tile;
@@ -221,7 +218,7 @@ __global__ void __launch_bounds__(BLOCK, 2) seg_pass_kernel(SegArgs a, int pass)
     const TileJob job{t, a.large_tile0[l], base, len,
                       a.seg_start + ((size_t)l * a.passes + pass) * RADIX,
                       a.status + (size_t)(pass & 1) * a.T * RADIX};
-    pass_tile<C, V, BLOCK, ITEMS, LB, RANK>(ra, pd, pass, job, key, val, s_k, s_v, ps, kdst, vdst,
+    pass_tile<C, V, BLOCK, ITEMS, LB, RANK, DPT>(ra, pd, pass, job, key, val, s_k, s_v, ps, kdst, vdst,
                                             NoAfterRank{});
 }
 
@@ -327,7 +324,8 @@ template <typename C, typename V>
 static int seg_launch(const SegPlan &p, SegArgs a, cudaStream_t s)
 {
     using Cfg = PassCfg<C, V>;
-    constexpr int BLOCK = Cfg::BLOCK, ITEMS = Cfg::ITEMS, LB = Cfg::LB, RANK = Cfg::RANK;
+    constexpr int BLOCK = Cfg::BLOCK, ITEMS = Cfg::ITEMS, LB = Cfg::LB, RANK = Cfg::RANK,
+                  DPT = Cfg::DPT;
     constexpr size_t TILE = (size_t)BLOCK * ITEMS;
     constexpr bool HAS_V = !std::is_same<V, NoVal>::value;
     const bool any_small = !p.warp.empty() || !p.small.empty() || !p.med.empty();
@@ -390,7 +388,7 @@ static int seg_launch(const SegPlan &p, SegArgs a, cudaStream_t s)
         XSS_LAUNCH(PK_SEG_MISC, s, (seg_scan_kernel<<<b.L, 256, 0, s>>>(b)));
         XSS_CUDA_TRY(cudaGetLastError());
         const size_t smem = TILE * (sizeof(C) + (HAS_V ? sizeof(V) : 0));
-        auto kern = seg_pass_kernel<C, V, BLOCK, ITEMS, LB, RANK>;
+        auto kern = seg_pass_kernel<C, V, BLOCK, ITEMS, LB, RANK, DPT>;
         static bool attr = false;
         if (!attr) {
             XSS_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,

@@ -15,6 +15,7 @@
 // second kernel moves list entries into holes.  Only misplaced elements are
 // written, as in an in-place quickselect partition.
 #include <algorithm>
+#include <cstring>
 #include <type_traits>
 #include "xss_internal.cuh"
 
@@ -91,32 +92,63 @@ __device__ __forceinline__ uint32_t warp_append(bool pred, unsigned int *counter
     return base + __popc(m & ((1u << lane) - 1u));
 }
 
+// One histogram round over every key (rounds 0, 1) or over the compacted
+// candidates (rounds >= 2).  16-byte vector loads, four per thread in
+// flight, keep enough bytes moving to cover memory latency; an unaligned
+// array takes the scalar loop.  Every loop bound is uniform across a warp so
+// the ballots of the round-1 compaction see all 32 lanes.
 template <typename C>
 __global__ void __launch_bounds__(256) sel_hist_kernel(SelArgs a, int round, int lo, int bits)
 {
+    constexpr int VW = 16 / sizeof(C);   // keys per vector
+    constexpr int U = 4;                 // vectors per thread in flight
     __shared__ uint32_t sh[SEL_BINS];
     const int nb = 1 << bits;
     for (int i = threadIdx.x; i < nb; i += 256) sh[i] = 0;
     __syncthreads();
     const C prefix = (C)a.st->prefix, mask = (C)a.st->mask;
     const size_t count = round <= 1 ? a.n : (size_t)a.st->cand_n;
-    const C *raw = static_cast<const C *>(a.keys);
+    const C *src = round <= 1 ? static_cast<const C *>(a.keys) : static_cast<const C *>(a.cand);
     C *cand = static_cast<C *>(a.cand);
+    const int lane = threadIdx.x & 31;
     const size_t stride = (size_t)gridDim.x * 256;
-    const size_t start = (size_t)blockIdx.x * 256 + threadIdx.x;
-    // loop bound rounded to whole warps so ballots see every lane (a warp's
-    // lanes hold 32 consecutive, 32-aligned indices)
-    const size_t bound = (count + 31) & ~(size_t)31;
-    for (size_t i = start; i < bound; i += stride) {
-        const bool active = i < count;
+    const size_t wbase = (size_t)blockIdx.x * 256 + threadIdx.x - lane;   // warp's first thread
+
+    auto visit = [&](C b, bool active) {
         C c = 0;
-        if (active) c = round <= 1 ? to_code(raw[i], a.xf) : cand[i];
+        if (active) c = round <= 1 ? to_code(b, a.xf) : b;
         const bool match = active && ((C)(c & mask) == prefix);
         if (match) atomicAdd(&sh[uint32_t(c >> lo) & (uint32_t)(nb - 1)], 1u);
         if (round == 1) {
             const uint32_t slot = warp_append(match, (unsigned int *)&a.st->cand_n);
             if (match) cand[slot] = c;
         }
+    };
+
+    size_t head = 0;
+    if ((reinterpret_cast<uintptr_t>(src) & 15) == 0) {
+        const size_t nvec = count / VW;
+        const uint4 *vsrc = reinterpret_cast<const uint4 *>(src);
+        for (size_t v0 = wbase; v0 < nvec; v0 += U * stride) {
+            uint4 w[U];
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                const size_t v = v0 + lane + u * stride;
+                w[u] = v < nvec ? vsrc[v] : make_uint4(0, 0, 0, 0);
+            }
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                const bool act = v0 + lane + u * stride < nvec;
+                const C *e = reinterpret_cast<const C *>(&w[u]);
+#pragma unroll
+                for (int j = 0; j < VW; ++j) visit(e[j], act);
+            }
+        }
+        head = nvec * VW;
+    }
+    for (size_t i0 = head + wbase; i0 < count; i0 += stride) {
+        const size_t i = i0 + lane;
+        visit(i < count ? src[i] : C(0), i < count);
     }
     __syncthreads();
     for (int i = threadIdx.x; i < nb; i += 256)
@@ -160,9 +192,54 @@ __global__ void __launch_bounds__(1024) sel_find_kernel(SelArgs a, int round, in
     if (round == 0 && t == 0) a.st->cand_n = 0;
 }
 
+// Block-wide exclusive scan of three 32-bit words per thread (each word
+// packs two 16-bit counters that cannot overflow within one chunk).
+__device__ __forceinline__ void sel_scan3(uint32_t (&v)[3], uint32_t (*s_w)[3], uint32_t (&tot)[3])
+{
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t x[3] = {v[0], v[1], v[2]};
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+#pragma unroll
+        for (int q = 0; q < 3; ++q) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, x[q], o);
+            if (lane >= o) x[q] += y;
+        }
+    }
+    if (lane == 31)
+        for (int q = 0; q < 3; ++q) s_w[warp][q] = x[q];
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+        uint32_t pre = 0, t = 0;
+        for (int w = 0; w < 8; ++w) {
+            const uint32_t c = s_w[w][q];
+            if (w < warp) pre += c;
+            t += c;
+        }
+        tot[q] = t;
+        v[q] = pre + x[q] - v[q];
+    }
+    __syncthreads();
+}
+
+// Partition bookkeeping: every element whose class (<, ==, > K) differs from
+// the region its position lies in goes to its class's list, its position to
+// its region's hole list.  A CTA takes chunks of 2048 elements, each thread
+// IPT consecutive ones (16-byte vector loads when the array is aligned), so
+// the lists come out in position order and the placing kernel's writes are
+// coalesced.  List slots are reserved with one global atomic per list per
+// chunk, and a chunk without misplaced elements skips that step.  The next
+// chunk's keys are loaded before the current chunk's scan, so reads stay in
+// flight across the chunk's barriers.
 template <typename C, typename V>
 __global__ void __launch_bounds__(256) sel_collect_kernel(SelArgs a)
 {
+    constexpr int IPT = 8, CH = 256 * IPT;
+    constexpr int NV = IPT * (int)sizeof(C) / 16;   // 16-byte vectors per thread
+    static_assert(IPT * sizeof(C) % 16 == 0, "whole vectors per thread");
+    __shared__ uint32_t s_w[8][3];
+    __shared__ uint32_t s_base[6];
     const C K = (C)a.st->prefix;
     const size_t cl = a.st->cl, ce = a.st->ce;
     const size_t regstart[3] = {0, cl, cl + ce};
@@ -171,39 +248,94 @@ __global__ void __launch_bounds__(256) sel_collect_kernel(SelArgs a)
     C *mis_k = static_cast<C *>(a.mis_k);
     V *mis_v = static_cast<V *>(a.mis_v);
     const size_t n = a.n;
-    const size_t stride = (size_t)gridDim.x * 256;
-    const size_t bound = (n + 31) & ~(size_t)31;
-    for (size_t p = (size_t)blockIdx.x * 256 + threadIdx.x; p < bound; p += stride) {
-        const bool active = p < n;
-        C raw = 0;
-        int cls = 0, reg = 0;
-        if (active) {
-            raw = keys[p];
-            const C c = to_code(raw, a.xf);
-            cls = c < K ? 0 : (c == K ? 1 : 2);
-            reg = p < cl ? 0 : (p < cl + ce ? 1 : 2);
-            if (a.op == SOP_ARG) a.out_idx[p] = p;
-        }
-        const bool mis = active && cls != reg;
-        const bool rec = mis && (a.op != SOP_KEYS || cls != 1);
+    const int tid = threadIdx.x;
+    const size_t gstride = (size_t)gridDim.x * CH;
+    const bool vec = (reinterpret_cast<uintptr_t>(keys) & 15) == 0;
+    C nxt[IPT];
+    auto load_chunk = [&](size_t c0) {
+        const size_t p0 = c0 + (size_t)tid * IPT;
+        if (vec && p0 + IPT <= n) {
+            uint4 q[NV];
+            const uint4 *src = reinterpret_cast<const uint4 *>(keys + p0);
 #pragma unroll
-        for (int X = 0; X < 3; ++X) {
-            const bool e = rec && cls == X;
-            const uint32_t slot = warp_append(e, &a.st->nmis[X]);
-            if (e && regstart[X] + slot < n) {
-                const size_t at = regstart[X] + slot;
-                if (a.op == SOP_ARG) {
-                    reinterpret_cast<uint32_t *>(a.mis_v)[at] = (uint32_t)p;
-                } else {
-                    mis_k[at] = raw;
-                    if constexpr (!std::is_same<V, uint8_t>::value)
-                        if (a.op == SOP_KV) mis_v[at] = vals[p];
+            for (int v = 0; v < NV; ++v) q[v] = src[v];
+            memcpy(nxt, q, sizeof(nxt));
+        } else {
+#pragma unroll
+            for (int j = 0; j < IPT; ++j) nxt[j] = p0 + j < n ? keys[p0 + j] : C(0);
+        }
+    };
+    load_chunk((size_t)blockIdx.x * CH);
+    for (size_t c0 = (size_t)blockIdx.x * CH; c0 < n; c0 += gstride) {
+        C raw[IPT];
+#pragma unroll
+        for (int j = 0; j < IPT; ++j) raw[j] = nxt[j];
+        if (c0 + gstride < n) load_chunk(c0 + gstride);
+        const size_t p0 = c0 + (size_t)tid * IPT;
+        uint8_t tag[IPT];   // bits 0-1: list class (3 = none), bits 2-3: hole region (3 = none)
+        uint32_t cnt[6] = {0, 0, 0, 0, 0, 0};
+        bool any = false;
+#pragma unroll
+        for (int j = 0; j < IPT; ++j) {
+            const size_t p = p0 + j;
+            uint32_t t = 0xF;
+            if (p < n) {
+                const C c = to_code(raw[j], a.xf);
+                const int cls = c < K ? 0 : (c == K ? 1 : 2);
+                const int reg = p < cl ? 0 : (p < cl + ce ? 1 : 2);
+                if (a.op == SOP_ARG) a.out_idx[p] = p;
+                if (cls != reg) {
+                    const bool rec = a.op != SOP_KEYS || cls != 1;
+                    t = (rec ? (uint32_t)cls : 3u) | ((uint32_t)reg << 2);
+                    any = true;
+                    // unrolled selects keep the counters in registers
+#pragma unroll
+                    for (int q = 0; q < 3; ++q) {
+                        cnt[q] += (rec && cls == q) ? 1u : 0u;
+                        cnt[3 + q] += reg == q ? 1u : 0u;
+                    }
                 }
             }
-            const bool h = mis && reg == X;
-            const uint32_t hslot = warp_append(h, &a.st->nhole[X]);
-            if (h && regstart[X] + hslot < n) a.holes[regstart[X] + hslot] = (uint32_t)p;
+            tag[j] = (uint8_t)t;
         }
+        if (!__syncthreads_or(any)) continue;
+        uint32_t w[3] = {cnt[0] | (cnt[1] << 16), cnt[2] | (cnt[3] << 16), cnt[4] | (cnt[5] << 16)};
+        uint32_t tot[3];
+        sel_scan3(w, s_w, tot);
+        if (tid < 6) {
+            const uint32_t t = (tot[tid >> 1] >> ((tid & 1) * 16)) & 0xFFFFu;
+            unsigned int *ctr = tid < 3 ? &a.st->nmis[tid] : &a.st->nhole[tid - 3];
+            s_base[tid] = t ? atomicAdd(ctr, t) : 0u;
+        }
+        __syncthreads();
+        uint32_t slot[6];
+#pragma unroll
+        for (int q = 0; q < 6; ++q) slot[q] = s_base[q] + ((w[q >> 1] >> ((q & 1) * 16)) & 0xFFFFu);
+#pragma unroll
+        for (int j = 0; j < IPT; ++j) {
+            const size_t p = p0 + j;
+            const uint32_t X = tag[j] & 3u, R = tag[j] >> 2;
+            size_t at_m = 0, at_h = 0;
+#pragma unroll
+            for (int q = 0; q < 3; ++q) {
+                if (X == (uint32_t)q) at_m = regstart[q] + slot[q]++;
+                if (R == (uint32_t)q) at_h = regstart[q] + slot[3 + q]++;
+            }
+            if (X != 3u) {
+                const size_t at = at_m;
+                if (at < n) {
+                    if (a.op == SOP_ARG) {
+                        reinterpret_cast<uint32_t *>(a.mis_v)[at] = (uint32_t)p;
+                    } else {
+                        mis_k[at] = raw[j];
+                        if constexpr (!std::is_same<V, uint8_t>::value)
+                            if (a.op == SOP_KV) mis_v[at] = vals[p];
+                    }
+                }
+            }
+            if (R != 3u && at_h < n) a.holes[at_h] = (uint32_t)p;
+        }
+        __syncthreads();   // s_base is rewritten by the next chunk
     }
 }
 
@@ -223,18 +355,31 @@ __global__ void __launch_bounds__(256) sel_place_kernel(SelArgs a)
         // counts are consistent by construction; clamp so a broken state can
         // never index past the lists
         const size_t cnt = min((size_t)a.st->nhole[X], a.n - regstart[X]);
-        for (size_t j = (size_t)blockIdx.x * 256 + threadIdx.x; j < cnt; j += stride) {
-            const uint32_t pos = a.holes[regstart[X] + j];
-            if (pos >= a.n) continue;
-            const size_t at = regstart[X] + j;
-            if (a.op == SOP_ARG) {
-                a.out_idx[pos] = reinterpret_cast<const uint32_t *>(a.mis_v)[at];
-            } else if (a.op == SOP_KEYS && X == 1) {
-                keys[pos] = kraw;
-            } else {
-                keys[pos] = mis_k[at];
-                if constexpr (!std::is_same<V, uint8_t>::value)
-                    if (a.op == SOP_KV) vals[pos] = mis_v[at];
+        // four list entries per thread in flight
+        constexpr int U = 4;
+        for (size_t j0 = (size_t)blockIdx.x * 256 + threadIdx.x; j0 < cnt; j0 += U * stride) {
+            uint32_t pos[U];
+            C mk[U];
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                const size_t j = j0 + u * stride;
+                pos[u] = j < cnt ? a.holes[regstart[X] + j] : 0xffffffffu;
+                mk[u] = (j < cnt && a.op == SOP_KEYS && X != 1) ? mis_k[regstart[X] + j] : C(0);
+            }
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                const size_t j = j0 + u * stride;
+                if (j >= cnt || pos[u] >= a.n) continue;
+                const size_t at = regstart[X] + j;
+                if (a.op == SOP_ARG) {
+                    a.out_idx[pos[u]] = reinterpret_cast<const uint32_t *>(a.mis_v)[at];
+                } else if (a.op == SOP_KEYS) {
+                    keys[pos[u]] = X == 1 ? kraw : mk[u];
+                } else {
+                    keys[pos[u]] = mis_k[at];
+                    if constexpr (!std::is_same<V, uint8_t>::value)
+                        if (a.op == SOP_KV) vals[pos[u]] = mis_v[at];
+                }
             }
         }
     }

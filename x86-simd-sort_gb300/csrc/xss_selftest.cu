@@ -12,11 +12,13 @@
 
 namespace xss {
 
-__global__ void __launch_bounds__(RADIX) selftest_lookback_kernel(const uint32_t *status,
-                                                                  unsigned *err, uint32_t limit)
+__global__ void __launch_bounds__(RADIX / 4) selftest_lookback_kernel(const uint32_t *status,
+                                                                      unsigned *err, uint32_t limit)
 {
-    // tile 1 of a two-tile pass whose tile 0 never publishes (all words zero)
-    (void)lookback_excl<16>(status, 1u, 0u, threadIdx.x, err, limit);
+    // tile 1 of a two-tile pass whose tile 0 never publishes (all words
+    // zero); four digits per thread as in the pass kernels' vector walk
+    uint32_t excl[4];
+    lookback_excl<8, 4>(status, 1u, 0u, threadIdx.x * 4, err, excl, limit);
 }
 
 __global__ void __launch_bounds__(32) selftest_mbar_kernel(unsigned *err, uint32_t limit)
@@ -44,7 +46,7 @@ extern "C" int xss_gpu_selftest_bounded_wait(int which, unsigned spin_limit, xss
     unsigned *err = static_cast<unsigned *>(ws);
     uint32_t *status = reinterpret_cast<uint32_t *>(static_cast<char *>(ws) + 256);
     XSS_CUDA_TRY(cudaMemsetAsync(ws, 0, 256 + 2 * RADIX * sizeof(uint32_t), s));
-    if (which == 0) selftest_lookback_kernel<<<1, RADIX, 0, s>>>(status, err, spin_limit);
+    if (which == 0) selftest_lookback_kernel<<<1, RADIX / 4, 0, s>>>(status, err, spin_limit);
     else if (which == 1) selftest_mbar_kernel<<<1, 32, 0, s>>>(err, spin_limit);
     else return XSS_EINVAL;
     XSS_CUDA_TRY(cudaGetLastError());
