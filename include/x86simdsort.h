@@ -198,6 +198,24 @@ void keyvalue_partial_sort(T1 *d_keys, T2 *d_vals, size_t k, size_t n, bool hasn
                                         d_vals, k, n, hasnan, descending, d_ws, ws_bytes,
                                         stream));
 }
+// Device form of object_qsort (lib/x86simdsort.h:73-106) for records whose key
+// is a data member: sorts n records of type T in device memory by
+// record.*key.  K must be a 32- or 64-bit key type, as in the host form.
+// Equal keys keep their input order.
+template <typename T, typename K>
+void object_qsort(T *d_arr, size_t n, K T::*key, bool hasnan = false, bool descending = false,
+                  xss_stream_t stream = nullptr, void *d_ws = nullptr, size_t ws_bytes = 0)
+{
+    static_assert(sizeof(K) == 4 || sizeof(K) == 8, "the key member must be 32 or 64 bits");
+    static_assert(std::is_trivially_copyable<T>::value, "records are moved as bytes");
+    // byte offset of the member, computed on suitably aligned raw storage
+    alignas(T) unsigned char probe[sizeof(T)];
+    const T *p = reinterpret_cast<const T *>(probe);
+    const size_t off = (size_t)(reinterpret_cast<const unsigned char *>(&(p->*key)) - probe);
+    check(xss_gpu_object_qsort(d_arr, n, sizeof(T), off, dtype_of<K>::value, hasnan, descending,
+                               d_ws, ws_bytes, stream));
+}
+
 // Wait for `stream` and report a device-side error latched by earlier calls.
 inline void synchronize(xss_stream_t stream = nullptr) { check(xss_gpu_stream_status(stream)); }
 

@@ -187,12 +187,28 @@ int xss_gpu_segmented_sort_percall(int key_dtype, int val_dtype, void *d_keys, v
                                    const uint64_t *h_offsets, size_t num_segments, int hasnan,
                                    int descending, xss_stream_t stream);
 
+/*
+ * Record sort on the device: sorts n records of rec_bytes bytes each in
+ * d_recs by the 32- or 64-bit key of type key_dtype stored at byte offset
+ * key_offset inside every record.  Device form of object_qsort
+ * (lib/x86simdsort.h:73-106) for keys that are a member of the record: the
+ * keys are read out on the GPU, sorted with the records' positions
+ * (key-value sort) and the records are gathered into sorted order.  Equal
+ * keys keep their input order.  Workspace: xss_gpu_object_workspace_size
+ * (holds a copy of the records), or NULL for the library's cached one.
+ */
+int xss_gpu_object_qsort(void *d_recs, size_t n, size_t rec_bytes, size_t key_offset,
+                         int key_dtype, int hasnan, int descending, void *d_ws,
+                         size_t ws_bytes, xss_stream_t stream);
+size_t xss_gpu_object_workspace_size(size_t n, size_t rec_bytes, int key_dtype);
+
 /* ------------------------------------------------------------------ */
 /* Instrumentation: per-kernel-kind launch counts (always on) and       */
 /* optional CUDA-event timing of every launch on its own stream.        */
 /* Kinds: 0 hist, 1 onesweep pass, 2 fixup, 3 small sort, 4 select      */
 /* histogram, 5 select find, 6 partition collect, 7 partition place,    */
-/* 8 segmented small, 9 segmented block, 10 segmented bookkeeping.      */
+/* 8 segmented small, 9 segmented block, 10 segmented bookkeeping,      */
+/* 11 record key extraction / gather.                                   */
 /* ------------------------------------------------------------------ */
 void xss_prof_enable(int on);
 void xss_prof_reset(void);

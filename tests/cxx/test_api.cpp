@@ -25,6 +25,14 @@ struct Point {
     double x, y;
 };
 
+// the record shape of the reference's example.c (object sort by a member)
+struct Rec {
+    int x;
+    int y;
+    float distance;
+    uint64_t metric;
+};
+
 int main()
 {
     std::mt19937 gen(0);
@@ -100,6 +108,35 @@ int main()
     CHECK(cudaMemcpy(c.data(), d_arr, c.size() * 4, cudaMemcpyDeviceToHost) == cudaSuccess);
     CHECK(c == cs);
     cudaFree(d_arr);
+
+    // device record sort by a member key; equal keys keep their input order
+    std::vector<Rec> recs(200000);
+    for (size_t i = 0; i < recs.size(); ++i)
+        recs[i] = {(int)i, (int)(gen() % 7), uni(gen), (uint64_t)(gen() % 5000)};
+    Rec *d_recs = nullptr;
+    CHECK(cudaMalloc(&d_recs, recs.size() * sizeof(Rec)) == cudaSuccess);
+    for (int by = 0; by < 2; ++by) {
+        CHECK(cudaMemcpy(d_recs, recs.data(), recs.size() * sizeof(Rec), cudaMemcpyHostToDevice) ==
+              cudaSuccess);
+        std::vector<Rec> want = recs;
+        if (by == 0) {
+            x86simdsort::gpu::object_qsort(d_recs, recs.size(), &Rec::metric);
+            std::stable_sort(want.begin(), want.end(),
+                             [](const Rec &l, const Rec &r) { return l.metric < r.metric; });
+        } else {
+            x86simdsort::gpu::object_qsort(d_recs, recs.size(), &Rec::distance, false, true);
+            std::stable_sort(want.begin(), want.end(),
+                             [](const Rec &l, const Rec &r) { return l.distance > r.distance; });
+        }
+        x86simdsort::gpu::synchronize();
+        std::vector<Rec> got(recs.size());
+        CHECK(cudaMemcpy(got.data(), d_recs, got.size() * sizeof(Rec), cudaMemcpyDeviceToHost) ==
+              cudaSuccess);
+        for (size_t i = 0; i < got.size(); ++i)   // member-wise: padding bytes are unspecified
+            CHECK(got[i].x == want[i].x && got[i].y == want[i].y &&
+                  got[i].distance == want[i].distance && got[i].metric == want[i].metric);
+    }
+    cudaFree(d_recs);
 
     // errors surface as exceptions (the reference has no error channel)
     bool threw = false;

@@ -33,8 +33,10 @@ static bool dtype_info(int dt, DtypeInfo &o)
     }
 }
 
-// Key-value pairs exist for 32/64-bit keys and values only
-// (lib/x86simdsort.cpp:274-293).
+// The reference has key-value sorts for 32/64-bit keys and values only
+// (lib/x86simdsort.cpp:274-293); here 16-bit keys (uint16, int16, _Float16)
+// may carry 32/64-bit values as well.  Values stay 32 or 64 bits.
+static bool kv_key_ok(int dt) { return dt >= XSS_DT_U16 && dt <= XSS_DT_F64; }
 static bool kv_type_ok(int dt) { return dt >= XSS_DT_U32 && dt <= XSS_DT_F64; }
 
 constexpr int MAX_DEV = 64;
@@ -221,7 +223,7 @@ static int kv_check(int kdt, int vdt, DtypeInfo &di)
     if (!dtype_info(kdt, di)) return XSS_EINVAL;
     DtypeInfo vi;
     if (!dtype_info(vdt, vi)) return XSS_EINVAL;
-    if (!kv_type_ok(kdt) || !kv_type_ok(vdt)) return XSS_EUNSUPPORTED;
+    if (!kv_key_ok(kdt) || !kv_type_ok(vdt)) return XSS_EUNSUPPORTED;
     return XSS_OK;
 }
 

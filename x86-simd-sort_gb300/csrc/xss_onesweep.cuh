@@ -165,11 +165,11 @@ __device__ __forceinline__ void lookback_excl(const uint32_t *st_pass, uint32_t 
 }
 
 // Shared-memory scratch of the per-tile body (static part).
-template <int BLOCK> struct PassSmem {
-    // Per-warp words per digit: the first half holds 32-bit digit counts,
-    // then running offsets; the second half (RANK 0) lane masks.  Zero
-    // between tiles.
-    unsigned long long wm[(BLOCK / 32) * RADIX];
+template <int BLOCK, int RANK> struct PassSmem {
+    // Per-warp words per digit: 32-bit digit counts, then running offsets;
+    // with RANK 0 followed by as many lane masks.  Zero between tiles.
+    static constexpr int WORDS = (BLOCK / 32) * RADIX * (RANK == 0 ? 2 : 1);
+    uint32_t wm[WORDS];
     int32_t off[RADIX];                     // global offset - local start, per digit
     uint32_t cnt[RADIX];                    // tile count per digit
     uint32_t lstart[RADIX];                 // tile-local start per digit
@@ -199,7 +199,7 @@ template <typename C, typename V, int BLOCK, int ITEMS, int LB, int RANK, int DP
 __device__ __forceinline__ void pass_tile(const RadixArgs &a, const PassDesc &pd, int pass,
                                           const TileJob &job, const C (&key)[ITEMS],
                                           const VS (&val)[ITEMS], C *s_k, VS *s_v,
-                                          PassSmem<BLOCK> &ps, C *kdst, V *vdst,
+                                          PassSmem<BLOCK, RANK> &ps, C *kdst, V *vdst,
                                           AfterRank after_rank)
 {
     constexpr int WARPS = BLOCK / 32;
@@ -210,7 +210,7 @@ __device__ __forceinline__ void pass_tile(const RadixArgs &a, const PassDesc &pd
     const uint32_t tile = job.tile;
     const int shift = pass * RADIX_BITS;
     const uint32_t tile_base = job.base;
-    uint32_t *const hist32 = reinterpret_cast<uint32_t *>(ps.wm);
+    uint32_t *const hist32 = ps.wm;
     uint32_t *wh = hist32 + warp * RADIX;
 
     // ---- per-warp digit counts (independent shared atomics)
@@ -330,7 +330,7 @@ __device__ __forceinline__ void pass_tile(const RadixArgs &a, const PassDesc &pd
             }
         }
     }
-    for (int i = tid; i < WARPS * RADIX; i += BLOCK) ps.wm[i] = 0;
+    for (int i = tid; i < PassSmem<BLOCK, RANK>::WORDS; i += BLOCK) ps.wm[i] = 0;
 }
 
 struct NoAfterRank {
@@ -350,14 +350,14 @@ __global__ void __launch_bounds__(BLOCK, MINB) onesweep_kernel(RadixArgs a, int 
     const PassDesc pd = a.hdr->desc[pass];
     if (!pd.active) return;
 
-    __shared__ PassSmem<BLOCK> ps;
+    __shared__ PassSmem<BLOCK, RANK> ps;
     __shared__ uint32_t s_tile;
     extern __shared__ __align__(128) unsigned char s_dyn[];
     C *s_k = reinterpret_cast<C *>(s_dyn);
     VS *s_v = reinterpret_cast<VS *>(s_dyn + TILE * sizeof(C));
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    for (int i = tid; i < (BLOCK / 32) * RADIX; i += BLOCK) ps.wm[i] = 0;
+    for (int i = tid; i < PassSmem<BLOCK, RANK>::WORDS; i += BLOCK) ps.wm[i] = 0;
     if (tid == 0) s_tile = atomicAdd(&a.hdr->tile_ctr[pass], 1u);
     __syncthreads();
     const uint32_t tile = s_tile;
@@ -417,7 +417,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) onesweep_persist_kernel(RadixArgs
     const PassDesc pd = a.hdr->desc[pass];
     if (!pd.active) return;
 
-    __shared__ PassSmem<BLOCK> ps;
+    __shared__ PassSmem<BLOCK, RANK> ps;
     __shared__ uint32_t s_tile[2];
     __shared__ __align__(8) uint64_t s_bar[2];
     extern __shared__ __align__(128) unsigned char s_dyn[];
@@ -450,7 +450,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) onesweep_persist_kernel(RadixArgs
     };
     auto by_tma = [&](uint32_t t) { return tma && t < num_tiles && (size_t)t * TILE + TILE <= n; };
 
-    for (int i = tid; i < (BLOCK / 32) * RADIX; i += BLOCK) ps.wm[i] = 0;
+    for (int i = tid; i < PassSmem<BLOCK, RANK>::WORDS; i += BLOCK) ps.wm[i] = 0;
     if (tid == 0) {
         mbar_init(&s_bar[0], 1);
         mbar_init(&s_bar[1], 1);

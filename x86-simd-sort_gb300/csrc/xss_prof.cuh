@@ -16,7 +16,8 @@ enum ProfKind : int {
     PK_SEG_SMALL = 8,  // segmented sort: many small segments per launch
     PK_SEG_BLOCK = 9,  // segmented sort: one CTA per medium segment
     PK_SEG_MISC = 10,  // segmented sort: binning / bookkeeping
-    PK_COUNT = 11
+    PK_OBJECT = 11,    // record sort: key extraction / record gather
+    PK_COUNT = 12
 };
 
 void prof_begin(cudaStream_t s, int kind);

@@ -158,13 +158,13 @@ __global__ void __launch_bounds__(BLOCK, 2) seg_pass_kernel(SegArgs a, int pass)
     constexpr int TILE = BLOCK * ITEMS;
     constexpr bool HAS_V = !std::is_same<V, NoVal>::value;
     using VS = typename std::conditional<HAS_V, V, uint8_t>::type;
-    __shared__ PassSmem<BLOCK> ps;
+    __shared__ PassSmem<BLOCK, RANK> ps;
     __shared__ uint32_t s_tile;
     extern __shared__ __align__(128) unsigned char s_dyn[];
     C *s_k = reinterpret_cast<C *>(s_dyn);
     VS *s_v = reinterpret_cast<VS *>(s_dyn + TILE * sizeof(C));
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    for (int i = tid; i < (BLOCK / 32) * RADIX; i += BLOCK) ps.wm[i] = 0;
+    for (int i = tid; i < PassSmem<BLOCK, RANK>::WORDS; i += BLOCK) ps.wm[i] = 0;
     if (tid == 0) s_tile = atomicAdd(&a.tile_ctr[pass], 1u);
     __syncthreads();
     const uint32_t t = s_tile;

@@ -72,6 +72,8 @@ _SIGS = {
     "xss_seg_plan_run": (_I, [_P, _P, _P, _P, _P, _Z, _P, _I]),
     "xss_seg_plan_destroy": (None, [_P]),
     "xss_gpu_segmented_sort_percall": (_I, [_I, _I, _P, _P, _P, _Z, _I, _I, _P]),
+    "xss_gpu_object_qsort": (_I, [_P, _Z, _Z, _Z, _I, _I, _I, _P, _Z, _P]),
+    "xss_gpu_object_workspace_size": (_Z, [_Z, _Z, _I]),
     "xss_prof_enable": (None, [_I]),
     "xss_prof_reset": (None, []),
     "xss_prof_read": (_I, [_I, ctypes.POINTER(ctypes.c_double),
@@ -81,7 +83,7 @@ _SIGS = {
 }
 
 PROF_KINDS = ["hist", "onesweep", "fixup", "small_sort", "sel_hist", "sel_find",
-              "sel_collect", "sel_place", "seg_small", "seg_block", "seg_misc"]
+              "sel_collect", "sel_place", "seg_small", "seg_block", "seg_misc", "object"]
 
 
 def prof_enable(on: bool) -> None:
@@ -273,6 +275,14 @@ def gpu_segmented_sort_percall(kdt, vdt, d_keys, d_vals, h_offsets: np.ndarray, 
                                                d_keys, d_vals or None, _ptr(h_offsets),
                                                h_offsets.size - 1, int(hasnan), int(descending),
                                                stream or None), "segmented_sort_percall")
+
+
+def gpu_object_qsort(d_recs, n, rec_bytes, key_offset, key_dtype, hasnan=False,
+                     descending=False, ws=0, ws_bytes=0, stream=0):
+    """Sort n records of rec_bytes bytes in device memory by the key at key_offset."""
+    check(lib().xss_gpu_object_qsort(d_recs, n, rec_bytes, key_offset, dtype_id(key_dtype),
+                                     int(hasnan), int(descending), ws or None, ws_bytes,
+                                     stream or None), "gpu_object_qsort")
 
 
 class SegPlan:
