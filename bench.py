@@ -51,12 +51,15 @@ def _peaks():
     return 6800.0, "fallback"
 
 
-def _traffic(workload):
-    p = os.path.join(ROOT, "profiles", "traffic.json")
-    if os.path.exists(p):
-        with open(p) as f:
-            return json.load(f).get(workload)
-    return None
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per launch of the
+# dominant kernel at the workload's full size: one ncu capture of a smaller case
+# scaled by the keys per launch (profiles/onesweep_kv_i64u64_2e24.md x16,
+# profiles/onesweep_f32_2e26.md x4).
+TRAFFIC = {"keyvalue_qsort": 7831007232, "qsort_f32": 1991962624}
+
+
+def _traffic(workload, n, n_full):
+    return TRAFFIC.get(workload) if n == n_full else None
 
 
 class Clocks:
@@ -111,6 +114,15 @@ class Workload:
 
     def __init__(self, torch, xss, n, stream):
         self.torch, self.xss, self.n, self.stream = torch, xss, n, stream
+        self._pinned = []
+
+    def pinned(self, nbytes: int, dtype) -> np.ndarray:
+        """Pinned host buffer viewed as `dtype`; the tensor that owns the memory is
+        kept alive with the workload (a dropped owner returns its block to torch's
+        host allocator, and copies from it then ran at half speed)."""
+        t = self.torch.empty(nbytes, dtype=self.torch.uint8, pin_memory=True)
+        self._pinned.append(t)
+        return t.numpy().view(dtype)
 
 
 class KeyValueSort(Workload):
@@ -166,8 +178,8 @@ class KeyValueSort(Workload):
         t = self.torch
         self.hk0 = self.k0.cpu().numpy()
         self.hv0 = self.v0.cpu().numpy().view(np.uint64)
-        self.hk = t.empty(self.n, dtype=t.int64, pin_memory=True).numpy()
-        self.hv = t.empty(self.n, dtype=t.int64, pin_memory=True).numpy().view(np.uint64)
+        self.hk = self.pinned(self.n * 8, np.int64)
+        self.hv = self.pinned(self.n * 8, np.uint64)
 
     def host_restore(self):
         np.copyto(self.hk, self.hk0)
@@ -235,7 +247,7 @@ class QsortF32(Workload):
 
     def host_setup(self):
         self.hk0 = self.k0.cpu().numpy()
-        self.hk = self.torch.empty(self.n, dtype=self.torch.float32, pin_memory=True).numpy()
+        self.hk = self.pinned(self.n * 4, np.float32)
 
     def host_restore(self):
         np.copyto(self.hk, self.hk0)
@@ -448,8 +460,7 @@ class ArgsortWorkload(Workload):
             self.n * (self.ib + self.kb)
 
     def host_setup(self):
-        self.hk = self.torch.empty(self.n * 8, dtype=self.torch.uint8, pin_memory=True).numpy() \
-            .view(np.dtype(self.kdt))
+        self.hk = self.pinned(self.n * 8, np.dtype(self.kdt))
         self.hk[:] = self.k0.cpu().numpy()
 
     def host_restore(self):
@@ -545,8 +556,7 @@ class SelectWorkload(Workload):
 
     def host_setup(self):
         self.hk0 = self.k0.cpu().numpy()
-        self.hk = self.torch.empty(self.n * 4, dtype=self.torch.uint8,
-                                   pin_memory=True).numpy().view(np.float32)
+        self.hk = self.pinned(self.n * 4, np.float32)
 
     def host_restore(self):
         np.copyto(self.hk, self.hk0)
@@ -619,6 +629,8 @@ def reference_arm(args):
     import torch  # noqa: F401  (only for the workload class' sample helpers)
     cls, n_full = WORKLOADS[args.workload]
     wl = cls(None, None, n_full, None)
+    if hasattr(wl, "partial"):
+        wl.k = args.k
     from oracle import pyoracle
     lib, kind = pyoracle.reference(), "reference"
     if lib is None:
@@ -642,8 +654,8 @@ def reference_arm(args):
             "vs_baseline": None,
             "dtype": DTYPE_OF[args.workload],
             "data": "synthetic",
-            "config": {"workload": f"{args.workload} (bounded CPU sample of {m} keys)",
-                       "full_n": n_full},
+            "config": {**wl.describe(), "parallelism": "replicas x1",
+                       "reference_sample": f"bounded CPU sample of {m} keys per step"},
             "cpu_baseline": {"value": val, "unit": "Gkeys/s",
                              "cores": threads if kind == "port" else min(16, os.cpu_count() or 1),
                              "kind": kind, "sample": f"{m} keys per step"},
@@ -955,7 +967,7 @@ def main():
         avg_pass_ms = ms_per_step
         achieved = wl.bytes_model() / (ms_per_step / 1e3) / 1e9
         active = launches / args.steps
-    traffic = _traffic(args.workload)
+    traffic = _traffic(args.workload, n, n_full)
 
     e2e = None
     if not args.no_e2e and rank == 0 and hasattr(wl, "host_run"):

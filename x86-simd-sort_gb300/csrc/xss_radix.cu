@@ -57,13 +57,15 @@ __global__ void __launch_bounds__(256) hist_kernel(RadixArgs a)
 #pragma unroll
         for (int u = 0; u < VEC; ++u) {
             const C c = to_code(e[u], a.xf);
-            for (int p = 0; p < P; ++p)
+#pragma unroll
+            for (int p = 0; p < (int)sizeof(C); ++p)
                 atomicAdd(&sh[p * RADIX + (uint32_t(c >> (p * RADIX_BITS)) & (RADIX - 1))], 1u);
         }
     }
     for (size_t i = nvec * VEC + gtid; i < n; i += stride) {
         const C c = to_code(src[i], a.xf);
-        for (int p = 0; p < P; ++p)
+#pragma unroll
+        for (int p = 0; p < (int)sizeof(C); ++p)
             atomicAdd(&sh[p * RADIX + (uint32_t(c >> (p * RADIX_BITS)) & (RADIX - 1))], 1u);
     }
 

@@ -152,8 +152,8 @@ __global__ void __launch_bounds__(256) seg_scan_kernel(SegArgs a)
 }
 
 // ---- large segments: one LSD pass over every large segment's tiles ----------
-template <typename C, typename V, int BLOCK, int ITEMS, int LB, int RANK, int DPT>
-__global__ void __launch_bounds__(BLOCK, 2) seg_pass_kernel(SegArgs a, int pass)
+template <typename C, typename V, int BLOCK, int ITEMS, int MINB, int LB, int RANK, int DPT>
+__global__ void __launch_bounds__(BLOCK, MINB) seg_pass_kernel(SegArgs a, int pass)
 {
     constexpr int TILE = BLOCK * ITEMS;
     constexpr bool HAS_V = !std::is_same<V, NoVal>::value;
@@ -242,12 +242,35 @@ struct SegPlan {
     unsigned long long graph_launches[PK_COUNT] = {};  // kernels per graph replay, by kind
 };
 
+// Pass lines (BLOCK, ITEMS, MINB, LB, RANK, PERSIST, DPT) of the large
+// class.  Its tiles run one CTA per tile across many segments, so it keeps
+// lines measured for that form (two CTAs per SM) instead of the resident
+// lines tuned for one whole array.
+#ifndef XSS_SEGCFG_KEYS
+#define XSS_SEGCFG_KEYS 512, 16, 2, 16, 0, 0, 0
+#endif
+#ifndef XSS_SEGCFG_K32V32
+#define XSS_SEGCFG_K32V32 512, 10, 2, 16, 1, 0, 0
+#endif
+#ifndef XSS_SEGCFG_DEFAULT
+#define XSS_SEGCFG_DEFAULT 256, 12, 2, 16, 1, 0, 0
+#endif
+template <typename C, typename V> struct SegPassCfg : CfgT<XSS_SEGCFG_DEFAULT> {};
+template <> struct SegPassCfg<uint16_t, NoVal> : CfgT<XSS_SEGCFG_KEYS> {};
+template <> struct SegPassCfg<uint32_t, NoVal> : CfgT<XSS_SEGCFG_KEYS> {};
+template <> struct SegPassCfg<uint32_t, uint32_t> : CfgT<XSS_SEGCFG_K32V32> {};
+
+template <typename C, typename V> constexpr size_t seg_tile()
+{
+    return (size_t)SegPassCfg<C, V>::BLOCK * SegPassCfg<C, V>::ITEMS;
+}
+
 static size_t seg_tile_size(int kb, int vb)
 {
     switch (kb) {
-    case 2: return vb == 0 ? pass_tile_size<uint16_t, NoVal>() : vb == 4 ? pass_tile_size<uint16_t, uint32_t>() : pass_tile_size<uint16_t, uint64_t>();
-    case 4: return vb == 0 ? pass_tile_size<uint32_t, NoVal>() : vb == 4 ? pass_tile_size<uint32_t, uint32_t>() : pass_tile_size<uint32_t, uint64_t>();
-    default: return vb == 0 ? pass_tile_size<uint64_t, NoVal>() : vb == 4 ? pass_tile_size<uint64_t, uint32_t>() : pass_tile_size<uint64_t, uint64_t>();
+    case 2: return vb == 0 ? seg_tile<uint16_t, NoVal>() : vb == 4 ? seg_tile<uint16_t, uint32_t>() : seg_tile<uint16_t, uint64_t>();
+    case 4: return vb == 0 ? seg_tile<uint32_t, NoVal>() : vb == 4 ? seg_tile<uint32_t, uint32_t>() : seg_tile<uint32_t, uint64_t>();
+    default: return vb == 0 ? seg_tile<uint64_t, NoVal>() : vb == 4 ? seg_tile<uint64_t, uint32_t>() : seg_tile<uint64_t, uint64_t>();
     }
 }
 
@@ -323,9 +346,9 @@ static int side_stream(SideStream *&out)
 template <typename C, typename V>
 static int seg_launch(const SegPlan &p, SegArgs a, cudaStream_t s)
 {
-    using Cfg = PassCfg<C, V>;
-    constexpr int BLOCK = Cfg::BLOCK, ITEMS = Cfg::ITEMS, LB = Cfg::LB, RANK = Cfg::RANK,
-                  DPT = Cfg::DPT;
+    using Cfg = SegPassCfg<C, V>;
+    constexpr int BLOCK = Cfg::BLOCK, ITEMS = Cfg::ITEMS, MINB = Cfg::MINB, LB = Cfg::LB,
+                  RANK = Cfg::RANK, DPT = Cfg::DPT;
     constexpr size_t TILE = (size_t)BLOCK * ITEMS;
     constexpr bool HAS_V = !std::is_same<V, NoVal>::value;
     const bool any_small = !p.warp.empty() || !p.small.empty() || !p.med.empty();
@@ -388,7 +411,7 @@ static int seg_launch(const SegPlan &p, SegArgs a, cudaStream_t s)
         XSS_LAUNCH(PK_SEG_MISC, s, (seg_scan_kernel<<<b.L, 256, 0, s>>>(b)));
         XSS_CUDA_TRY(cudaGetLastError());
         const size_t smem = TILE * (sizeof(C) + (HAS_V ? sizeof(V) : 0));
-        auto kern = seg_pass_kernel<C, V, BLOCK, ITEMS, LB, RANK, DPT>;
+        auto kern = seg_pass_kernel<C, V, BLOCK, ITEMS, MINB, LB, RANK, DPT>;
         static bool attr = false;
         if (!attr) {
             XSS_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,

@@ -225,24 +225,24 @@ __device__ __forceinline__ void sel_scan3(uint32_t (&v)[3], uint32_t (*s_w)[3], 
 
 // Partition bookkeeping: every element whose class (<, ==, > K) differs from
 // the region its position lies in goes to its class's list, its position to
-// its region's hole list.  A CTA takes chunks of 2048 elements, each thread
-// IPT consecutive ones (16-byte vector loads when the array is aligned), so
-// the lists come out in position order and the placing kernel's writes are
-// coalesced.  List slots are reserved with one global atomic per list per
-// chunk, and a chunk without misplaced elements skips that step.  The next
-// chunk's keys are loaded before the current chunk's scan, so reads stay in
-// flight across the chunk's barriers.
+// its region's hole list.  A CTA takes chunks of 256 * IPT elements, each
+// thread IPT consecutive ones (8 16-bit or 32 bytes of wider keys; 16-byte
+// vector loads when the array is aligned), so the lists come out in position
+// order and the placing
+// kernel's writes are coalesced.  The six per-thread list counters live in
+// 16-bit fields of two 64-bit words; list slots are reserved with one global
+// atomic per list per chunk, and a chunk without misplaced elements skips
+// that step.  The next chunk's keys are loaded before the current chunk's
+// scan, so reads stay in flight across the chunk's barriers.
 template <typename C, typename V>
 __global__ void __launch_bounds__(256) sel_collect_kernel(SelArgs a)
 {
-    constexpr int IPT = 8, CH = 256 * IPT;
+    constexpr int IPT = sizeof(C) >= 4 ? 32 / (int)sizeof(C) : 8, CH = 256 * IPT;
     constexpr int NV = IPT * (int)sizeof(C) / 16;   // 16-byte vectors per thread
-    static_assert(IPT * sizeof(C) % 16 == 0, "whole vectors per thread");
     __shared__ uint32_t s_w[8][3];
-    __shared__ uint32_t s_base[6];
+    __shared__ unsigned long long s_base[6];
     const C K = (C)a.st->prefix;
     const size_t cl = a.st->cl, ce = a.st->ce;
-    const size_t regstart[3] = {0, cl, cl + ce};
     const C *keys = static_cast<const C *>(a.keys);
     const V *vals = static_cast<const V *>(a.vals);
     C *mis_k = static_cast<C *>(a.mis_k);
@@ -272,57 +272,50 @@ __global__ void __launch_bounds__(256) sel_collect_kernel(SelArgs a)
         for (int j = 0; j < IPT; ++j) raw[j] = nxt[j];
         if (c0 + gstride < n) load_chunk(c0 + gstride);
         const size_t p0 = c0 + (size_t)tid * IPT;
-        uint8_t tag[IPT];   // bits 0-1: list class (3 = none), bits 2-3: hole region (3 = none)
-        uint32_t cnt[6] = {0, 0, 0, 0, 0, 0};
-        bool any = false;
+        uint32_t tags = 0;                      // 4 bits per element: list class, hole region
+        unsigned long long cm = 0, ch = 0;      // 16-bit counters: lists 0..2 / holes 0..2
 #pragma unroll
         for (int j = 0; j < IPT; ++j) {
             const size_t p = p0 + j;
             uint32_t t = 0xF;
             if (p < n) {
                 const C c = to_code(raw[j], a.xf);
-                const int cls = c < K ? 0 : (c == K ? 1 : 2);
-                const int reg = p < cl ? 0 : (p < cl + ce ? 1 : 2);
+                const uint32_t cls = (uint32_t)(c >= K) + (uint32_t)(c > K);
+                const uint32_t reg = (uint32_t)(p >= cl) + (uint32_t)(p >= cl + ce);
                 if (a.op == SOP_ARG) a.out_idx[p] = p;
                 if (cls != reg) {
                     const bool rec = a.op != SOP_KEYS || cls != 1;
-                    t = (rec ? (uint32_t)cls : 3u) | ((uint32_t)reg << 2);
-                    any = true;
-                    // unrolled selects keep the counters in registers
-#pragma unroll
-                    for (int q = 0; q < 3; ++q) {
-                        cnt[q] += (rec && cls == q) ? 1u : 0u;
-                        cnt[3 + q] += reg == q ? 1u : 0u;
-                    }
+                    t = (rec ? cls : 3u) | (reg << 2);
+                    cm += rec ? (1ull << (16 * cls)) : 0ull;
+                    ch += 1ull << (16 * reg);
                 }
             }
-            tag[j] = (uint8_t)t;
+            tags |= t << (4 * j);
         }
-        if (!__syncthreads_or(any)) continue;
-        uint32_t w[3] = {cnt[0] | (cnt[1] << 16), cnt[2] | (cnt[3] << 16), cnt[4] | (cnt[5] << 16)};
+        if (!__syncthreads_or((cm | ch) != 0ull)) continue;
+        uint32_t w[3] = {(uint32_t)cm, (uint32_t)(cm >> 32) | ((uint32_t)ch << 16),
+                         (uint32_t)(ch >> 16)};
         uint32_t tot[3];
         sel_scan3(w, s_w, tot);
         if (tid < 6) {
             const uint32_t t = (tot[tid >> 1] >> ((tid & 1) * 16)) & 0xFFFFu;
             unsigned int *ctr = tid < 3 ? &a.st->nmis[tid] : &a.st->nhole[tid - 3];
-            s_base[tid] = t ? atomicAdd(ctr, t) : 0u;
+            const size_t rs = (tid % 3) == 0 ? 0 : ((tid % 3) == 1 ? cl : cl + ce);
+            s_base[tid] = rs + (t ? atomicAdd(ctr, t) : 0u);
         }
         __syncthreads();
-        uint32_t slot[6];
-#pragma unroll
-        for (int q = 0; q < 6; ++q) slot[q] = s_base[q] + ((w[q >> 1] >> ((q & 1) * 16)) & 0xFFFFu);
+        // this thread's first slot in each list: chunk base + exclusive prefix
+        unsigned long long om = (unsigned long long)w[0] | ((unsigned long long)(w[1] & 0xFFFFu) << 32);
+        unsigned long long oh = (unsigned long long)(w[1] >> 16) | ((unsigned long long)w[2] << 16);
+        const unsigned long long bm0 = s_base[0], bm1 = s_base[1], bm2 = s_base[2];
+        const unsigned long long bh0 = s_base[3], bh1 = s_base[4], bh2 = s_base[5];
 #pragma unroll
         for (int j = 0; j < IPT; ++j) {
             const size_t p = p0 + j;
-            const uint32_t X = tag[j] & 3u, R = tag[j] >> 2;
-            size_t at_m = 0, at_h = 0;
-#pragma unroll
-            for (int q = 0; q < 3; ++q) {
-                if (X == (uint32_t)q) at_m = regstart[q] + slot[q]++;
-                if (R == (uint32_t)q) at_h = regstart[q] + slot[3 + q]++;
-            }
+            const uint32_t X = (tags >> (4 * j)) & 3u, R = (tags >> (4 * j + 2)) & 3u;
             if (X != 3u) {
-                const size_t at = at_m;
+                const size_t at = (X == 0 ? bm0 : X == 1 ? bm1 : bm2) + ((om >> (16 * X)) & 0xFFFFu);
+                om += 1ull << (16 * X);
                 if (at < n) {
                     if (a.op == SOP_ARG) {
                         reinterpret_cast<uint32_t *>(a.mis_v)[at] = (uint32_t)p;
@@ -333,7 +326,11 @@ __global__ void __launch_bounds__(256) sel_collect_kernel(SelArgs a)
                     }
                 }
             }
-            if (R != 3u && at_h < n) a.holes[at_h] = (uint32_t)p;
+            if (R != 3u) {
+                const size_t at = (R == 0 ? bh0 : R == 1 ? bh1 : bh2) + ((oh >> (16 * R)) & 0xFFFFu);
+                oh += 1ull << (16 * R);
+                if (at < n) a.holes[at] = (uint32_t)p;
+            }
         }
         __syncthreads();   // s_base is rewritten by the next chunk
     }
