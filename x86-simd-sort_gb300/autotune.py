@@ -1,14 +1,16 @@
 """Offline autotuner for the onesweep radix pass.
 
 Each (key width, value width) class of the pass kernel has a tuning line
-``XSS_CFG_<class> BLOCK, ITEMS, MINB, LB, RANK, PERSIST, DPT`` (meaning of
-each field: the comment above ``CfgT`` in ``csrc/xss_onesweep.cuh``).  This
+``XSS_CFG_<class> BLOCK, ITEMS, MINB, LB, RANK, PERSIST, DPT`` for large
+arrays and ``XSS_CFGM_<class>`` for arrays up to ``XSS_MID_N`` keys (class
+names ending in ``_MID``; meaning of each field: the comment above ``CfgT``
+in ``csrc/xss_onesweep.cuh``).  This
 tool builds one library per candidate line (the candidate is pre-included as
 a header, so the sources stay untouched), times each on the GPU with CUDA
 events on full-size uniform inputs, checks every result, and writes the
 fastest line per class to a header::
 
-    python x86-simd-sort_gb300/autotune.py --classes K32,K64V64 --out xss_tuning.h
+    python x86-simd-sort_gb300/autotune.py --classes K32,K64V64,K32_MID --out xss_tuning.h
 
 Copy the written header to ``csrc/xss_tuning.h``; ``xss_onesweep.cuh``
 includes it when present, so the next build uses the tuned lines.  Timing
@@ -51,7 +53,22 @@ CANDIDATES = {
     "K32V32": ["512,10,2,16,0,0,1", "512,12,1,16,0,1,1", "512,14,1,16,1,1,1"],
     "K64V64": ["512,11,1,16,1,1,1", "512,12,1,16,1,1,1", "512,10,1,16,0,1,1", "512,6,2,16,1,0,1"],
     "DEFAULT": ["512,12,1,16,0,1,1", "512,14,1,16,0,1,1", "512,12,1,16,1,1,1", "512,6,2,16,0,0,1"],
+    # mid-size arrays: several CTAs per SM (tile or resident form)
+    "K16_MID": ["512,16,2,16,0,1,0", "256,16,3,16,0,1,0", "256,8,4,16,0,0,0"],
+    "K32_MID": ["512,16,2,16,0,1,0", "256,16,3,16,0,1,0", "256,8,4,16,0,0,0", "512,8,2,16,0,0,1",
+                "320,20,3,16,0,1,0"],
+    "K64_MID": ["256,16,2,16,1,1,0", "256,8,3,16,1,0,0", "512,8,2,16,0,1,1"],
+    "K32V32_MID": ["512,10,2,16,1,0,0", "256,8,3,16,1,0,0", "512,6,2,16,1,0,1"],
+    "K64V64_MID": ["256,12,2,16,1,0,0", "256,6,3,16,1,0,0", "512,6,2,16,1,0,1"],
+    "DEFAULT_MID": ["256,12,2,16,1,0,0", "512,6,2,16,0,0,1", "256,8,3,16,1,0,0"],
 }
+
+
+def _base(cls: str):
+    """(width class, macro name, is mid-size) of a class name."""
+    mid = cls.endswith("_MID")
+    base = cls[:-4] if mid else cls
+    return base, ("XSS_CFGM_" if mid else "XSS_CFG_") + base, mid
 
 
 def _run(cmd, **kw):
@@ -66,7 +83,7 @@ def build_variant(cls: str, line: str, common_objs: list) -> str:
     tag = f"{cls}_{line.replace(',', '_')}"
     hdr = os.path.join(TUNE_DIR, f"cfg_{tag}.h")
     with open(hdr, "w") as f:
-        f.write(f"#define XSS_CFG_{cls} {line}\n")
+        f.write(f"#define {_base(cls)[1]} {line}\n")
     obj = os.path.join(TUNE_DIR, f"radix_{tag}.o")
     _run([_build.NVCC] + _build.ARCH + _build.NVCC_FLAGS +
          ["--pre-include", hdr, "-c", os.path.join(_build.CSRC, "xss_radix.cu"), "-o", obj])
@@ -90,7 +107,7 @@ def measure(cls: str, n: int, reps: int) -> dict:
     """Child-process side: time the class's sort with the library in XSS_LIB."""
     import torch
     import pyxss
-    kdt, vdt = CLASSES[cls]
+    kdt, vdt = CLASSES[_base(cls)[0]]
     tdt = {"uint16": torch.int16, "uint32": torch.int32, "uint64": torch.int64}
     kb = {"uint16": 2, "uint32": 4, "uint64": 8}[kdt]
     g = torch.Generator(device="cuda").manual_seed(7)
@@ -143,7 +160,8 @@ def main():
     ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
     ap.add_argument("--classes", default="K32,K64V64")
     ap.add_argument("--candidates", default="", help="CLASS=line;CLASS=line overrides")
-    ap.add_argument("--n", type=int, default=1 << 28)
+    ap.add_argument("--n", type=int, default=1 << 28, help="keys for large-array classes")
+    ap.add_argument("--n-mid", type=int, default=1 << 21, help="keys for _MID classes")
     ap.add_argument("--reps", type=int, default=5)
     ap.add_argument("--out", default=os.path.join(PKG, "_build", "xss_tuning.h"))
     ap.add_argument("--measure", default="", help=argparse.SUPPRESS)
@@ -171,8 +189,10 @@ def main():
     results = {}
     for (c, line), so in zip(jobs, libs):
         env = dict(os.environ, XSS_LIB=so)
+        mid = _base(c)[2]
         r = subprocess.run([sys.executable, os.path.abspath(__file__), "--measure", c,
-                            "--n", str(args.n), "--reps", str(args.reps)],
+                            "--n", str(args.n_mid if mid else args.n),
+                            "--reps", str(args.reps * 4 if mid else args.reps)],
                            env=env, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
         try:
             res = json.loads(r.stdout.strip().splitlines()[-1])
@@ -183,7 +203,7 @@ def main():
 
     with open(args.out, "w") as f:
         f.write("// xss_tuning.h -- onesweep pass lines chosen by autotune.py "
-                f"(n = {args.n}, uniform keys, median of {args.reps} sorts).\n")
+                f"(n = {args.n}, _MID classes n = {args.n_mid}; uniform keys; median time).\n")
         f.write("// Each line: BLOCK, ITEMS, MINB, LB, RANK, PERSIST, DPT.\n#pragma once\n")
         for c, rs in results.items():
             good = [(line, r) for line, r in rs if r["ok"]]
@@ -192,7 +212,8 @@ def main():
             best, br = min(good, key=lambda x: x[1]["ms"])
             f.write("\n// " + c + ": " + "; ".join(
                 f"{line} {r['ms']:.3f} ms" for line, r in rs) + "\n")
-            f.write(f"#ifndef XSS_CFG_{c}\n#define XSS_CFG_{c} {best.replace(',', ', ')}\n#endif\n")
+            macro = _base(c)[1]
+            f.write(f"#ifndef {macro}\n#define {macro} {best.replace(',', ', ')}\n#endif\n")
     print("wrote", args.out)
 
 

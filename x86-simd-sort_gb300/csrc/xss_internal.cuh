@@ -86,6 +86,11 @@ int radix_select(int op, int kbytes, KeyXform xf, void *keys, void *vals, int vb
 
 int num_sms();
 
+// Per host thread: sort arrays of every size with the mid-size pass lines
+// (several CTAs per SM), so kernels of concurrent requests on other streams
+// share the SMs.  The serving loop's scheduler thread sets it.
+void set_prefer_shared_sm(bool on);
+
 // Library-owned scratch for (current device, stream), grown on demand.
 int cached_workspace(cudaStream_t s, size_t bytes, void **out);
 

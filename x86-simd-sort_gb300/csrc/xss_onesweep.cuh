@@ -99,9 +99,46 @@ template <> struct PassCfg<uint64_t, NoVal> : CfgT<XSS_CFG_K64> {};
 template <> struct PassCfg<uint32_t, uint32_t> : CfgT<XSS_CFG_K32V32> {};
 template <> struct PassCfg<uint64_t, uint64_t> : CfgT<XSS_CFG_K64V64> {};
 
+// Size class: arrays of at most XSS_MID_N keys use the XSS_CFGM_* lines.
+// Those keep several CTAs per SM in the tile or resident form, so a grid of
+// one or two waves stays busy and sorts on other streams (a serving loop)
+// can run beside them; the lines above are for large arrays, where one
+// resident CTA per SM with a prefetched tile moves the most bytes.
+#ifndef XSS_MID_N
+#define XSS_MID_N (size_t(1) << 24)
+#endif
+#ifndef XSS_CFGM_DEFAULT
+#define XSS_CFGM_DEFAULT 256, 12, 2, 16, 1, 0, 0
+#endif
+#ifndef XSS_CFGM_K16
+#define XSS_CFGM_K16 512, 16, 2, 16, 0, 1, 0
+#endif
+#ifndef XSS_CFGM_K32
+#define XSS_CFGM_K32 512, 16, 2, 16, 0, 1, 0
+#endif
+#ifndef XSS_CFGM_K64
+#define XSS_CFGM_K64 256, 16, 2, 16, 1, 1, 0
+#endif
+#ifndef XSS_CFGM_K32V32
+#define XSS_CFGM_K32V32 512, 10, 2, 16, 1, 0, 0
+#endif
+#ifndef XSS_CFGM_K64V64
+#define XSS_CFGM_K64V64 256, 12, 2, 16, 1, 0, 0
+#endif
+template <typename C, typename V> struct PassCfgMid : CfgT<XSS_CFGM_DEFAULT> {};
+template <> struct PassCfgMid<uint16_t, NoVal> : CfgT<XSS_CFGM_K16> {};
+template <> struct PassCfgMid<uint32_t, NoVal> : CfgT<XSS_CFGM_K32> {};
+template <> struct PassCfgMid<uint64_t, NoVal> : CfgT<XSS_CFGM_K64> {};
+template <> struct PassCfgMid<uint32_t, uint32_t> : CfgT<XSS_CFGM_K32V32> {};
+template <> struct PassCfgMid<uint64_t, uint64_t> : CfgT<XSS_CFGM_K64V64> {};
+
 template <typename C, typename V> constexpr size_t pass_tile_size()
 {
     return (size_t)PassCfg<C, V>::BLOCK * PassCfg<C, V>::ITEMS;
+}
+template <typename C, typename V> constexpr size_t pass_tile_size_mid()
+{
+    return (size_t)PassCfgMid<C, V>::BLOCK * PassCfgMid<C, V>::ITEMS;
 }
 
 // Exclusive prefixes of DPT consecutive digits d0.. over tiles [first, tile)

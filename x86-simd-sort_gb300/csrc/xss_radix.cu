@@ -183,20 +183,34 @@ static RadixLayout radix_layout(int op, int kbytes, int vbytes, size_t n, size_t
     return L;
 }
 
-static size_t tile_for_bytes(int op, int kbytes, int vbytes)
+static thread_local bool t_prefer_shared_sm = false;
+void set_prefer_shared_sm(bool on) { t_prefer_shared_sm = on; }
+
+static bool use_mid_lines(size_t n) { return n <= XSS_MID_N || t_prefer_shared_sm; }
+
+// Tile of the lines a sort of n keys may use: for n above XSS_MID_N both
+// classes are possible (see set_prefer_shared_sm), so the workspace is sized
+// for the smaller tile, which needs the larger look-back array.
+template <typename C, typename V> static size_t tile_of(size_t n)
+{
+    return n <= XSS_MID_N ? pass_tile_size_mid<C, V>()
+                          : std::min(pass_tile_size_mid<C, V>(), pass_tile_size<C, V>());
+}
+
+static size_t tile_for_bytes(int op, int kbytes, int vbytes, size_t n)
 {
     const int vb = (op == SOP_ARG) ? 4 : (op == SOP_KV ? vbytes : 0);
     switch (kbytes) {
-    case 2: return vb == 0 ? pass_tile_size<uint16_t, NoVal>() : vb == 4 ? pass_tile_size<uint16_t, uint32_t>() : pass_tile_size<uint16_t, uint64_t>();
-    case 4: return vb == 0 ? pass_tile_size<uint32_t, NoVal>() : vb == 4 ? pass_tile_size<uint32_t, uint32_t>() : pass_tile_size<uint32_t, uint64_t>();
-    default: return vb == 0 ? pass_tile_size<uint64_t, NoVal>() : vb == 4 ? pass_tile_size<uint64_t, uint32_t>() : pass_tile_size<uint64_t, uint64_t>();
+    case 2: return vb == 0 ? tile_of<uint16_t, NoVal>(n) : vb == 4 ? tile_of<uint16_t, uint32_t>(n) : tile_of<uint16_t, uint64_t>(n);
+    case 4: return vb == 0 ? tile_of<uint32_t, NoVal>(n) : vb == 4 ? tile_of<uint32_t, uint32_t>(n) : tile_of<uint32_t, uint64_t>(n);
+    default: return vb == 0 ? tile_of<uint64_t, NoVal>(n) : vb == 4 ? tile_of<uint64_t, uint32_t>(n) : tile_of<uint64_t, uint64_t>(n);
     }
 }
 
 size_t radix_workspace_bytes(int op, int kbytes, int vbytes, size_t n)
 {
     if (n <= SMALL_SORT_MAX) return 0;
-    return radix_layout(op, kbytes, vbytes, n, tile_for_bytes(op, kbytes, vbytes)).total;
+    return radix_layout(op, kbytes, vbytes, n, tile_for_bytes(op, kbytes, vbytes, n)).total;
 }
 
 // How a sort is launched: where device-side errors go and whether launches
@@ -278,12 +292,35 @@ static int resident_passes(const RadixArgs &a, int sms, cudaStream_t s, const La
     return XSS_OK;
 }
 
-template <typename C, typename V>
-static int onesweep_launch(int op, KeyXform xf, void *keys, void *vals, uint64_t *out_idx,
-                           size_t n, void *ws, size_t ws_bytes, cudaStream_t s,
-                           const LaunchOpts &o)
+// One CTA per tile for every active pass.
+template <typename C, typename V, int BLOCK, int ITEMS, int MINB, int LB, int RANK, int DPT>
+static int tile_passes(const RadixArgs &a, cudaStream_t s, const LaunchOpts &o)
 {
-    using Cfg = PassCfg<C, V>;
+    constexpr size_t TILE = (size_t)BLOCK * ITEMS;
+    constexpr bool HAS_V = !std::is_same<V, NoVal>::value;
+    const size_t smem = TILE * (sizeof(C) + (HAS_V ? sizeof(V) : 0));
+    auto kern = onesweep_kernel<C, V, BLOCK, ITEMS, MINB, LB, RANK, DPT>;
+    static bool attr_set = false;
+    if (!attr_set) {
+        XSS_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)smem));
+        attr_set = true;
+    }
+    for (int p = 0; p < a.passes; ++p) {
+        XSS_LAUNCH_OPT(o, PK_ONESWEEP, s, kern<<<a.num_tiles, BLOCK, smem, s>>>(a, p));
+        XSS_CUDA_TRY(cudaGetLastError());
+    }
+    return XSS_OK;
+}
+
+// LARGE: the large-array lines, whose launch form may also be forced through
+// XSS_ONESWEEP; otherwise the mid-size lines in their own form only.
+template <typename C, typename V, bool LARGE>
+static int onesweep_launch_cls(int op, KeyXform xf, void *keys, void *vals, uint64_t *out_idx,
+                               size_t n, void *ws, size_t ws_bytes, cudaStream_t s,
+                               const LaunchOpts &o)
+{
+    using Cfg = typename std::conditional<LARGE, PassCfg<C, V>, PassCfgMid<C, V>>::type;
     constexpr int BLOCK = Cfg::BLOCK, ITEMS = Cfg::ITEMS, MINB = Cfg::MINB, LB = Cfg::LB,
                   RANK = Cfg::RANK, DPT = Cfg::DPT;
     constexpr size_t TILE = (size_t)BLOCK * ITEMS;
@@ -319,30 +356,32 @@ static int onesweep_launch(int op, KeyXform xf, void *keys, void *vals, uint64_t
     XSS_LAUNCH_OPT(o, PK_HIST, s, hist_kernel<C><<<hist_grid, 256, 0, s>>>(a));
     XSS_CUDA_TRY(cudaGetLastError());
 
-    const size_t vsz = HAS_V ? sizeof(V) : 0;
-    const int form = pass_form(Cfg::PERSIST);
-    if (form != 0) {
-        const int rc = form == 1
-            ? resident_passes<C, V, BLOCK, ITEMS, MINB, LB, RANK, DPT, true>(a, sms, s, o)
-            : resident_passes<C, V, BLOCK, ITEMS, MINB, LB, RANK, DPT, false>(a, sms, s, o);
-        if (rc) return rc;
+    const int form = LARGE ? pass_form(Cfg::PERSIST) : Cfg::PERSIST;
+    int rc = XSS_OK;
+    if (form == 1) {
+        if constexpr (LARGE || Cfg::PERSIST == 1)
+            rc = resident_passes<C, V, BLOCK, ITEMS, MINB, LB, RANK, DPT, true>(a, sms, s, o);
+    } else if (form == 2) {
+        if constexpr (LARGE || Cfg::PERSIST == 2)
+            rc = resident_passes<C, V, BLOCK, ITEMS, MINB, LB, RANK, DPT, false>(a, sms, s, o);
     } else {
-        const size_t smem = TILE * (sizeof(C) + vsz);
-        auto kern = onesweep_kernel<C, V, BLOCK, ITEMS, MINB, LB, RANK, DPT>;
-        static bool attr_set = false;
-        if (!attr_set) {
-            XSS_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                              (int)smem));
-            attr_set = true;
-        }
-        for (int p = 0; p < a.passes; ++p) {
-            XSS_LAUNCH_OPT(o, PK_ONESWEEP, s, kern<<<a.num_tiles, BLOCK, smem, s>>>(a, p));
-            XSS_CUDA_TRY(cudaGetLastError());
-        }
+        if constexpr (LARGE || Cfg::PERSIST == 0)
+            rc = tile_passes<C, V, BLOCK, ITEMS, MINB, LB, RANK, DPT>(a, s, o);
     }
+    if (rc) return rc;
     XSS_LAUNCH_OPT(o, PK_FIXUP, s, fixup_kernel<C, V><<<sms * 2, 256, 0, s>>>(a));
     XSS_CUDA_TRY(cudaGetLastError());
     return XSS_OK;
+}
+
+template <typename C, typename V>
+static int onesweep_launch(int op, KeyXform xf, void *keys, void *vals, uint64_t *out_idx,
+                           size_t n, void *ws, size_t ws_bytes, cudaStream_t s,
+                           const LaunchOpts &o)
+{
+    return use_mid_lines(n)
+               ? onesweep_launch_cls<C, V, false>(op, xf, keys, vals, out_idx, n, ws, ws_bytes, s, o)
+               : onesweep_launch_cls<C, V, true>(op, xf, keys, vals, out_idx, n, ws, ws_bytes, s, o);
 }
 
 template <typename C>

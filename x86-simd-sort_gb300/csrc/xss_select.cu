@@ -228,12 +228,12 @@ __device__ __forceinline__ void sel_scan3(uint32_t (&v)[3], uint32_t (*s_w)[3], 
 // its region's hole list.  A CTA takes chunks of 256 * IPT elements, each
 // thread IPT consecutive ones (8 16-bit or 32 bytes of wider keys; 16-byte
 // vector loads when the array is aligned), so the lists come out in position
-// order and the placing
-// kernel's writes are coalesced.  The six per-thread list counters live in
-// 16-bit fields of two 64-bit words; list slots are reserved with one global
-// atomic per list per chunk, and a chunk without misplaced elements skips
-// that step.  The next chunk's keys are loaded before the current chunk's
-// scan, so reads stay in flight across the chunk's barriers.
+// order and the placing kernel's writes are coalesced.  Per element the work
+// is 32-bit: region bounds relative to the thread's first element, six list
+// counters in 4-bit fields of one word.  List slots are reserved with one
+// global atomic per list per chunk, and a chunk without misplaced elements
+// skips that step.  The next chunk's keys are loaded before the current
+// chunk's scan, so reads stay in flight across the chunk's barriers.
 template <typename C, typename V>
 __global__ void __launch_bounds__(256) sel_collect_kernel(SelArgs a)
 {
@@ -272,64 +272,79 @@ __global__ void __launch_bounds__(256) sel_collect_kernel(SelArgs a)
         for (int j = 0; j < IPT; ++j) raw[j] = nxt[j];
         if (c0 + gstride < n) load_chunk(c0 + gstride);
         const size_t p0 = c0 + (size_t)tid * IPT;
+        // region boundaries relative to this thread's first element, clamped
+        // to [0, IPT], so the per-element region test is 32-bit
+        const uint32_t r1 = (uint32_t)(cl > p0 ? min(cl - p0, (size_t)IPT) : 0);
+        const uint32_t r2 = (uint32_t)(cl + ce > p0 ? min(cl + ce - p0, (size_t)IPT) : 0);
+        const uint32_t valid = (uint32_t)(n > p0 ? min(n - p0, (size_t)IPT) : 0);
         uint32_t tags = 0;                      // 4 bits per element: list class, hole region
-        unsigned long long cm = 0, ch = 0;      // 16-bit counters: lists 0..2 / holes 0..2
+        uint32_t cnt4 = 0;                      // 4-bit counters: lists 0..2, holes 0..2
 #pragma unroll
         for (int j = 0; j < IPT; ++j) {
-            const size_t p = p0 + j;
             uint32_t t = 0xF;
-            if (p < n) {
+            if ((uint32_t)j < valid) {
                 const C c = to_code(raw[j], a.xf);
                 const uint32_t cls = (uint32_t)(c >= K) + (uint32_t)(c > K);
-                const uint32_t reg = (uint32_t)(p >= cl) + (uint32_t)(p >= cl + ce);
-                if (a.op == SOP_ARG) a.out_idx[p] = p;
+                const uint32_t reg = (uint32_t)((uint32_t)j >= r1) + (uint32_t)((uint32_t)j >= r2);
+                if (a.op == SOP_ARG) a.out_idx[p0 + j] = p0 + j;
                 if (cls != reg) {
                     const bool rec = a.op != SOP_KEYS || cls != 1;
                     t = (rec ? cls : 3u) | (reg << 2);
-                    cm += rec ? (1ull << (16 * cls)) : 0ull;
-                    ch += 1ull << (16 * reg);
+                    cnt4 += (rec ? (1u << (4 * cls)) : 0u) + (1u << (4 * (3 + reg)));
                 }
             }
             tags |= t << (4 * j);
         }
-        if (!__syncthreads_or((cm | ch) != 0ull)) continue;
-        uint32_t w[3] = {(uint32_t)cm, (uint32_t)(cm >> 32) | ((uint32_t)ch << 16),
-                         (uint32_t)(ch >> 16)};
+        if (!__syncthreads_or(cnt4 != 0u)) continue;
+        // two 16-bit counters per scanned word
+        uint32_t w[3];
+#pragma unroll
+        for (int q = 0; q < 3; ++q)
+            w[q] = ((cnt4 >> (8 * q)) & 0xFu) | (((cnt4 >> (8 * q + 4)) & 0xFu) << 16);
         uint32_t tot[3];
         sel_scan3(w, s_w, tot);
         if (tid < 6) {
             const uint32_t t = (tot[tid >> 1] >> ((tid & 1) * 16)) & 0xFFFFu;
             unsigned int *ctr = tid < 3 ? &a.st->nmis[tid] : &a.st->nhole[tid - 3];
             const size_t rs = (tid % 3) == 0 ? 0 : ((tid % 3) == 1 ? cl : cl + ce);
-            s_base[tid] = rs + (t ? atomicAdd(ctr, t) : 0u);
+            // a list that would run past the array (never, with consistent
+            // counts) is not written for this chunk
+            const size_t at = rs + (t ? atomicAdd(ctr, t) : 0u);
+            s_base[tid] = at + t <= n ? at : ~0ull;
         }
         __syncthreads();
         // this thread's first slot in each list: chunk base + exclusive prefix
-        unsigned long long om = (unsigned long long)w[0] | ((unsigned long long)(w[1] & 0xFFFFu) << 32);
-        unsigned long long oh = (unsigned long long)(w[1] >> 16) | ((unsigned long long)w[2] << 16);
-        const unsigned long long bm0 = s_base[0], bm1 = s_base[1], bm2 = s_base[2];
-        const unsigned long long bh0 = s_base[3], bh1 = s_base[4], bh2 = s_base[5];
+        size_t slot[6];
+        bool ok[6];
+#pragma unroll
+        for (int q = 0; q < 6; ++q) {
+            const unsigned long long b0 = s_base[q];
+            ok[q] = b0 != ~0ull;
+            slot[q] = b0 + ((w[q >> 1] >> ((q & 1) * 16)) & 0xFFFFu);
+        }
 #pragma unroll
         for (int j = 0; j < IPT; ++j) {
             const size_t p = p0 + j;
             const uint32_t X = (tags >> (4 * j)) & 3u, R = (tags >> (4 * j + 2)) & 3u;
-            if (X != 3u) {
-                const size_t at = (X == 0 ? bm0 : X == 1 ? bm1 : bm2) + ((om >> (16 * X)) & 0xFFFFu);
-                om += 1ull << (16 * X);
-                if (at < n) {
-                    if (a.op == SOP_ARG) {
-                        reinterpret_cast<uint32_t *>(a.mis_v)[at] = (uint32_t)p;
-                    } else {
-                        mis_k[at] = raw[j];
-                        if constexpr (!std::is_same<V, uint8_t>::value)
-                            if (a.op == SOP_KV) mis_v[at] = vals[p];
+#pragma unroll
+            for (int q = 0; q < 3; ++q) {
+                if (X == (uint32_t)q) {
+                    if (ok[q]) {
+                        const size_t at = slot[q];
+                        if (a.op == SOP_ARG) {
+                            reinterpret_cast<uint32_t *>(a.mis_v)[at] = (uint32_t)p;
+                        } else {
+                            mis_k[at] = raw[j];
+                            if constexpr (!std::is_same<V, uint8_t>::value)
+                                if (a.op == SOP_KV) mis_v[at] = vals[p];
+                        }
                     }
+                    ++slot[q];
                 }
-            }
-            if (R != 3u) {
-                const size_t at = (R == 0 ? bh0 : R == 1 ? bh1 : bh2) + ((oh >> (16 * R)) & 0xFFFFu);
-                oh += 1ull << (16 * R);
-                if (at < n) a.holes[at] = (uint32_t)p;
+                if (R == (uint32_t)q) {
+                    if (ok[3 + q]) a.holes[slot[3 + q]] = (uint32_t)p;
+                    ++slot[3 + q];
+                }
             }
         }
         __syncthreads();   // s_base is rewritten by the next chunk

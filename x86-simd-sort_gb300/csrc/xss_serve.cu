@@ -441,6 +441,7 @@ struct xss_server_s {
     void run()
     {
         cudaSetDevice(device);
+        set_prefer_shared_sm(true);   // requests on several streams share the SMs
         while (true) {
             {
                 std::unique_lock<std::mutex> lk(mu);

@@ -31,3 +31,34 @@
 #ifndef XSS_CFG_DEFAULT
 #define XSS_CFG_DEFAULT 512, 14, 1, 16, 0, 1, 1
 #endif
+
+// mid-size classes
+// K16_MID: 512,16,2,16,0,1,0 0.056 ms; 256,16,3,16,0,1,0 0.060 ms; 256,8,4,16,0,0,0 0.066 ms
+#ifndef XSS_CFGM_K16
+#define XSS_CFGM_K16 512, 16, 2, 16, 0, 1, 0
+#endif
+
+// K32_MID: 512,16,2,16,0,1,0 0.093 ms; 256,16,3,16,0,1,0 0.101 ms; 256,8,4,16,0,0,0 0.109 ms; 512,8,2,16,0,0,1 0.100 ms; 320,20,3,16,0,1,0 0.107 ms
+#ifndef XSS_CFGM_K32
+#define XSS_CFGM_K32 512, 16, 2, 16, 0, 1, 0
+#endif
+
+// K64_MID: 256,16,2,16,1,1,0 0.198 ms; 256,8,3,16,1,0,0 0.204 ms; 512,8,2,16,0,1,1 0.197 ms
+#ifndef XSS_CFGM_K64
+#define XSS_CFGM_K64 512, 8, 2, 16, 0, 1, 1
+#endif
+
+// K32V32_MID: 512,10,2,16,1,0,0 0.114 ms; 256,8,3,16,1,0,0 0.119 ms; 512,6,2,16,1,0,1 0.117 ms
+#ifndef XSS_CFGM_K32V32
+#define XSS_CFGM_K32V32 512, 10, 2, 16, 1, 0, 0
+#endif
+
+// K64V64_MID: 256,12,2,16,1,0,0 0.250 ms; 256,6,3,16,1,0,0 0.261 ms; 512,6,2,16,1,0,1 0.246 ms
+#ifndef XSS_CFGM_K64V64
+#define XSS_CFGM_K64V64 512, 6, 2, 16, 1, 0, 1
+#endif
+
+// DEFAULT_MID: 256,12,2,16,1,0,0 0.238 ms; 512,6,2,16,0,0,1 0.227 ms; 256,8,3,16,1,0,0 0.231 ms
+#ifndef XSS_CFGM_DEFAULT
+#define XSS_CFGM_DEFAULT 512, 6, 2, 16, 0, 0, 1
+#endif
