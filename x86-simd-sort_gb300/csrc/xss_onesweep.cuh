@@ -58,8 +58,7 @@ __device__ __forceinline__ void *pick3(void *const (&b)[3], int i)
 //   BLOCK, ITEMS: threads and keys per thread (tile = BLOCK * ITEMS)
 //   MINB:         CTAs per SM the register budget is cut for
 //   LB:           predecessors probed per look-back round trip
-//   RANK:         1 = peer masks from eight ballots, 0 = from shared atomicOr,
-//                 3 = from the warp match instruction
+//   RANK:         1 = peer masks from eight ballots, 0 = from shared atomicOr
 //   PERSIST:      0 = one CTA per tile, 1 = resident CTAs with TMA prefetch,
 //                 2 = resident CTAs with ordinary loads (one staging buffer)
 //   DPT:          look-back placement.  0: after ranking, one digit per
@@ -308,8 +307,8 @@ __device__ __forceinline__ void pass_tile(const RadixArgs &a, const PassDesc &pd
     // The lanes sharing a digit find each other either by eight ballots, one
     // per digit bit (RANK 1: no shared memory, consecutive items overlap), or
     // through a per-warp word per digit that each lane sets its bit in and
-    // reads back (RANK 0: fewer instructions, the leader clears the word), or
-    // by the warp match instruction (RANK 3).
+    // reads back (RANK 0: fewer instructions, the leader clears the word).
+    // (The warp match instruction measured 1.8x slower than either.)
     // The highest such lane advances the warp's running offset for the digit.
     {
         const uint32_t lt_mask = (1u << lane) - 1u;
@@ -325,8 +324,6 @@ __device__ __forceinline__ void pass_tile(const RadixArgs &a, const PassDesc &pd
                     const uint32_t m = __ballot_sync(0xffffffffu, set);
                     peers &= set ? m : ~m;
                 }
-            } else if constexpr (RANK == 3) {
-                peers = __match_any_sync(0xffffffffu, d);
             } else {
                 atomicOr(&mt[d], 1u << lane);
                 __syncwarp();
@@ -336,9 +333,15 @@ __device__ __forceinline__ void pass_tile(const RadixArgs &a, const PassDesc &pd
             const int leader = 31 - __clz(peers);
             uint32_t base = 0;
             if (lane == leader) {
-                base = wh[d];
-                wh[d] = base + __popc(peers);
-                if constexpr (RANK == 0) mt[d] = 0;
+                if constexpr (RANK == 0) {
+                    // one shared atomic instead of a load and a store (measured
+                    // faster with shared-memory masks, slower with ballots)
+                    base = atomicAdd(&wh[d], (uint32_t)__popc(peers));
+                    mt[d] = 0;
+                } else {
+                    base = wh[d];
+                    wh[d] = base + __popc(peers);
+                }
             }
             base = __shfl_sync(0xffffffffu, base, leader);
             const uint32_t p = base + __popc(peers & lt_mask);

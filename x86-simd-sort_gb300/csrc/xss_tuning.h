@@ -1,64 +1,63 @@
-// xss_tuning.h -- onesweep pass lines chosen by autotune.py (n = 268435456, uniform keys, median of 5 sorts).
+// xss_tuning.h -- onesweep pass lines chosen by autotune.py (n = 268435456, _MID classes n = 2097152; uniform keys; median time).
 // Each line: BLOCK, ITEMS, MINB, LB, RANK, PERSIST, DPT.
 #pragma once
 
-// K16: 256,24,3,16,0,1,0 2.360 ms; 512,16,2,16,0,1,0 2.427 ms; 320,20,3,16,0,1,0 2.309 ms
+// K16: 320,20,3,16,0,1,0 2.153 ms; 256,24,3,16,0,1,0 2.273 ms; 512,16,2,16,0,1,0 2.252 ms
 #ifndef XSS_CFG_K16
 #define XSS_CFG_K16 320, 20, 3, 16, 0, 1, 0
 #endif
 
-// K32: 320,20,3,16,0,1,0 4.648 ms; 256,24,3,16,0,1,0 4.732 ms; 512,16,2,16,0,1,0 4.819 ms; 384,16,3,16,0,1,0 5.252 ms
+// K32: 320,20,3,16,0,1,0 4.389 ms; 256,24,3,16,0,1,0 4.605 ms; 512,16,2,16,0,1,0 4.532 ms; 320,24,2,16,0,1,0 4.816 ms
 #ifndef XSS_CFG_K32
 #define XSS_CFG_K32 320, 20, 3, 16, 0, 1, 0
 #endif
 
-// K64: 256,16,2,16,0,1,0 13.416 ms; 512,12,1,16,0,1,1 13.400 ms; 512,16,1,16,0,1,1 12.773 ms; 512,8,2,16,0,1,1 13.602 ms
+// K64: 512,16,1,16,0,1,1 12.669 ms; 512,12,1,16,0,1,1 13.474 ms; 256,16,2,16,0,1,0 13.229 ms
 #ifndef XSS_CFG_K64
 #define XSS_CFG_K64 512, 16, 1, 16, 0, 1, 1
 #endif
 
-// K32V32: 512,10,2,16,0,0,1 7.852 ms; 512,12,1,16,0,1,1 7.349 ms; 512,14,1,16,1,1,1 7.499 ms
+// K32V32: 512,12,1,16,0,1,1 7.319 ms; 512,10,2,16,0,0,1 7.644 ms; 512,14,1,16,0,1,1 6.999 ms
 #ifndef XSS_CFG_K32V32
-#define XSS_CFG_K32V32 512, 12, 1, 16, 0, 1, 1
+#define XSS_CFG_K32V32 512, 14, 1, 16, 0, 1, 1
 #endif
 
-// K64V64: 512,11,1,16,1,1,1 18.000 ms; 512,12,1,16,1,1,1 19.056 ms; 512,10,1,16,0,1,1 18.231 ms; 512,6,2,16,1,0,1 21.274 ms
+// K64V64: 512,11,1,16,1,1,1 17.939 ms; 512,11,1,16,0,1,1 17.538 ms; 512,10,1,16,0,1,1 18.100 ms; 512,12,1,16,0,1,1 inf ms
 #ifndef XSS_CFG_K64V64
-#define XSS_CFG_K64V64 512, 11, 1, 16, 1, 1, 1
+#define XSS_CFG_K64V64 512, 11, 1, 16, 0, 1, 1
 #endif
 
-// DEFAULT: 512,12,1,16,0,1,1 16.129 ms; 512,14,1,16,0,1,1 15.672 ms; 512,12,1,16,1,1,1 16.723 ms; 512,6,2,16,0,0,1 20.688 ms
+// DEFAULT: 512,14,1,16,0,1,1 15.387 ms; 512,12,1,16,0,1,1 15.975 ms; 512,14,1,16,1,1,1 17.137 ms
 #ifndef XSS_CFG_DEFAULT
 #define XSS_CFG_DEFAULT 512, 14, 1, 16, 0, 1, 1
 #endif
 
-// mid-size classes
-// K16_MID: 512,16,2,16,0,1,0 0.056 ms; 256,16,3,16,0,1,0 0.060 ms; 256,8,4,16,0,0,0 0.066 ms
+// K16_MID: 512,16,2,16,0,1,0 0.057 ms; 256,16,3,16,0,1,0 0.060 ms
 #ifndef XSS_CFGM_K16
 #define XSS_CFGM_K16 512, 16, 2, 16, 0, 1, 0
 #endif
 
-// K32_MID: 512,16,2,16,0,1,0 0.093 ms; 256,16,3,16,0,1,0 0.101 ms; 256,8,4,16,0,0,0 0.109 ms; 512,8,2,16,0,0,1 0.100 ms; 320,20,3,16,0,1,0 0.107 ms
+// K32_MID: 512,16,2,16,0,1,0 0.092 ms; 256,16,3,16,0,1,0 0.100 ms; 512,8,2,16,0,0,1 0.100 ms
 #ifndef XSS_CFGM_K32
 #define XSS_CFGM_K32 512, 16, 2, 16, 0, 1, 0
 #endif
 
-// K64_MID: 256,16,2,16,1,1,0 0.198 ms; 256,8,3,16,1,0,0 0.204 ms; 512,8,2,16,0,1,1 0.197 ms
+// K64_MID: 512,8,2,16,0,1,1 0.196 ms; 256,16,2,16,1,1,0 0.198 ms; 256,16,2,16,0,1,0 0.199 ms
 #ifndef XSS_CFGM_K64
 #define XSS_CFGM_K64 512, 8, 2, 16, 0, 1, 1
 #endif
 
-// K32V32_MID: 512,10,2,16,1,0,0 0.114 ms; 256,8,3,16,1,0,0 0.119 ms; 512,6,2,16,1,0,1 0.117 ms
+// K32V32_MID: 512,10,2,16,1,0,0 0.115 ms; 512,10,2,16,0,0,0 0.114 ms; 512,6,2,16,1,0,1 0.119 ms
 #ifndef XSS_CFGM_K32V32
-#define XSS_CFGM_K32V32 512, 10, 2, 16, 1, 0, 0
+#define XSS_CFGM_K32V32 512, 10, 2, 16, 0, 0, 0
 #endif
 
-// K64V64_MID: 256,12,2,16,1,0,0 0.250 ms; 256,6,3,16,1,0,0 0.261 ms; 512,6,2,16,1,0,1 0.246 ms
+// K64V64_MID: 512,6,2,16,1,0,1 0.242 ms; 512,6,2,16,0,0,1 0.240 ms; 256,12,2,16,1,0,0 0.246 ms
 #ifndef XSS_CFGM_K64V64
-#define XSS_CFGM_K64V64 512, 6, 2, 16, 1, 0, 1
+#define XSS_CFGM_K64V64 512, 6, 2, 16, 0, 0, 1
 #endif
 
-// DEFAULT_MID: 256,12,2,16,1,0,0 0.238 ms; 512,6,2,16,0,0,1 0.227 ms; 256,8,3,16,1,0,0 0.231 ms
+// DEFAULT_MID: 512,6,2,16,0,0,1 0.228 ms; 256,12,2,16,1,0,0 0.235 ms; 256,8,3,16,1,0,0 0.228 ms
 #ifndef XSS_CFGM_DEFAULT
 #define XSS_CFGM_DEFAULT 512, 6, 2, 16, 0, 0, 1
 #endif
