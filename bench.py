@@ -53,9 +53,9 @@ def _peaks():
 
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per launch of the
 # dominant kernel at the workload's full size: one ncu capture of a smaller case
-# scaled by the keys per launch (profiles/onesweep_kv_i64u64_2e24.md x16,
+# scaled by the keys per launch (profiles/onesweep_kv_i64u64_2e25.md x8,
 # profiles/onesweep_f32_2e26.md x4).
-TRAFFIC = {"keyvalue_qsort": 7831007232, "qsort_f32": 1991962624}
+TRAFFIC = {"keyvalue_qsort": 8245047296, "qsort_f32": 1991735296}
 
 
 def _traffic(workload, n, n_full):
@@ -972,7 +972,8 @@ def main():
     e2e = None
     if not args.no_e2e and rank == 0 and hasattr(wl, "host_run"):
         wl.host_setup()
-        for _ in range(1):
+        # the same W warm-up steps as the device leg
+        for _ in range(max(args.warmup, 3)):
             wl.host_restore()
             wl.host_run()
         t = 0.0

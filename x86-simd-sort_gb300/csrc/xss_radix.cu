@@ -24,24 +24,32 @@ namespace xss {
 // fused with clearing the look-back status words.  The last CTA to finish
 // turns the histograms into per-pass bucket starts and writes the pass plan:
 // a pass whose digit is the same for every key is skipped.
-// Lanes count into four copies of the histograms (lane & 3), so a digit that
-// most keys share (the top byte of floats, small-range integers) costs at
-// most an 8-way same-address conflict instead of 32-way; the copies sit 8
-// banks apart.
-constexpr int HIST_COPIES = 4;
-constexpr int HIST_COPY_STRIDE = MAX_PASSES * RADIX + 8;
+// Lanes count into eight interleaved copies of the histograms: counter
+// (pass p, digit d, copy c) is word (p * RADIX + d) * 8 + c and lane l uses
+// copy l & 7.  A copy's words all lie in the four banks c, c+8, c+16, c+24,
+// which only the four lanes of that copy touch: random digits meet at most
+// 4-way bank conflicts (32 lanes over 32 banks average about 3.5), and a
+// digit every key shares (the top byte of floats, small-range integers)
+// costs a 4-way same-address conflict instead of 32-way.  The counters live
+// in dynamic shared memory (sizeof(C) * 8 KiB).
+constexpr int HIST_COPIES = 8;
+template <typename C> constexpr size_t hist_smem_bytes()
+{
+    return sizeof(C) * RADIX * HIST_COPIES * sizeof(uint32_t);
+}
 template <typename C>
 __global__ void __launch_bounds__(256) hist_kernel(RadixArgs a)
 {
-    __shared__ uint32_t sh_all[HIST_COPIES * HIST_COPY_STRIDE];
+    extern __shared__ __align__(16) uint32_t sh_all[];
     __shared__ uint32_t s_scan[8];
     __shared__ int s_last;
     __shared__ int s_active[MAX_PASSES];
     const int tid = threadIdx.x;
     const int P = a.passes;
-    for (int i = tid; i < HIST_COPIES * HIST_COPY_STRIDE; i += 256) sh_all[i] = 0;
+    constexpr int NW = (int)sizeof(C) * RADIX * HIST_COPIES;
+    for (int i = tid; i < NW; i += 256) sh_all[i] = 0;
     __syncthreads();
-    uint32_t *const sh = sh_all + (tid & (HIST_COPIES - 1)) * HIST_COPY_STRIDE;
+    uint32_t *const sh = sh_all + (tid & (HIST_COPIES - 1));
 
     const C *src = static_cast<const C *>(a.kbuf[0]);
     const size_t n = a.n;
@@ -59,14 +67,16 @@ __global__ void __launch_bounds__(256) hist_kernel(RadixArgs a)
             const C c = to_code(e[u], a.xf);
 #pragma unroll
             for (int p = 0; p < (int)sizeof(C); ++p)
-                atomicAdd(&sh[p * RADIX + (uint32_t(c >> (p * RADIX_BITS)) & (RADIX - 1))], 1u);
+                atomicAdd(&sh[(p * RADIX + (uint32_t(c >> (p * RADIX_BITS)) & (RADIX - 1))) *
+                              HIST_COPIES], 1u);
         }
     }
     for (size_t i = nvec * VEC + gtid; i < n; i += stride) {
         const C c = to_code(src[i], a.xf);
 #pragma unroll
         for (int p = 0; p < (int)sizeof(C); ++p)
-            atomicAdd(&sh[p * RADIX + (uint32_t(c >> (p * RADIX_BITS)) & (RADIX - 1))], 1u);
+            atomicAdd(&sh[(p * RADIX + (uint32_t(c >> (p * RADIX_BITS)) & (RADIX - 1))) *
+                          HIST_COPIES], 1u);
     }
 
     // clear the look-back words of every pass (multiple of 4 words, 16B aligned)
@@ -76,9 +86,9 @@ __global__ void __launch_bounds__(256) hist_kernel(RadixArgs a)
 
     __syncthreads();
     for (int i = tid; i < P * RADIX; i += 256) {
-        uint32_t t = 0;
-#pragma unroll
-        for (int c = 0; c < HIST_COPIES; ++c) t += sh_all[c * HIST_COPY_STRIDE + i];
+        const uint4 *w = reinterpret_cast<const uint4 *>(sh_all + i * HIST_COPIES);
+        const uint4 x = w[0], y = w[1];
+        const uint32_t t = x.x + x.y + x.z + x.w + y.x + y.y + y.z + y.w;
         if (t) atomicAdd(&a.hdr->hist[0][0] + i, t);
     }
     __threadfence();
@@ -353,7 +363,14 @@ static int onesweep_launch_cls(int op, KeyXform xf, void *keys, void *vals, uint
     const int sms = num_sms();
     const size_t want = (n + 256 * 16 - 1) / (256 * 16);
     const int hist_grid = (int)std::max<size_t>(1, std::min<size_t>(want, (size_t)sms * 8));
-    XSS_LAUNCH_OPT(o, PK_HIST, s, hist_kernel<C><<<hist_grid, 256, 0, s>>>(a));
+    constexpr size_t HSMEM = hist_smem_bytes<C>();
+    static bool hist_attr = false;
+    if (!hist_attr) {
+        XSS_CUDA_TRY(cudaFuncSetAttribute(hist_kernel<C>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)HSMEM));
+        hist_attr = true;
+    }
+    XSS_LAUNCH_OPT(o, PK_HIST, s, hist_kernel<C><<<hist_grid, 256, HSMEM, s>>>(a));
     XSS_CUDA_TRY(cudaGetLastError());
 
     const int form = LARGE ? pass_form(Cfg::PERSIST) : Cfg::PERSIST;
