@@ -930,6 +930,13 @@ def main():
         stream.synchronize()
         dom_ms, dom_launches = xss.prof_read(wl.dominant)
         dom_steps = 1
+        # per-kind breakdown from the same ungraphed run (kinds on the side
+        # stream overlap the others, so the entries may sum past ms_per_step)
+        for kind in xss.PROF_KINDS:
+            k_ms, k_n = xss.prof_read(kind)
+            if k_n:
+                kernels[kind] = {"ms_per_step": k_ms, "launches_per_step": k_n,
+                                 "from": "one run without graph replay"}
     xss.prof_enable(False)
     xss.stream_status(stream.cuda_stream)
     checked = wl.check()

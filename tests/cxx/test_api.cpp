@@ -12,6 +12,7 @@
 #include <vector>
 
 #include "x86simdsort.h"
+#include "x86simdsort-static-incl.h"
 
 #define CHECK(c)                                                             \
     do {                                                                     \
@@ -137,6 +138,24 @@ int main()
                   got[i].distance == want[i].distance && got[i].metric == want[i].metric);
     }
     cudaFree(d_recs);
+
+    // the header-only static API (namespace x86simdsortStatic), NumPy's argsort form
+    {
+        std::vector<double> sv(70000);
+        for (auto &x : sv) x = nd(gen);
+        std::vector<double> sref = sv;
+        std::vector<size_t> sarg(sv.size());
+        x86simdsortStatic::argsort(sv.data(), sarg.data(), sv.size());
+        std::sort(sref.begin(), sref.end());
+        for (size_t i = 0; i < sv.size(); ++i) CHECK(sv[sarg[i]] == sref[i]);
+        x86simdsortStatic::qsort(sv.data(), sv.size());
+        CHECK(sv == sref);
+        std::vector<uint32_t> kk(5000), vv(5000);
+        for (size_t i = 0; i < kk.size(); ++i) { kk[i] = (uint32_t)(gen() % 97); vv[i] = (uint32_t)i; }
+        std::vector<uint32_t> k0 = kk;
+        x86simdsortStatic::keyvalue_qsort(kk.data(), vv.data(), kk.size());
+        for (size_t i = 0; i < kk.size(); ++i) CHECK(k0[vv[i]] == kk[i] && (i == 0 || kk[i - 1] <= kk[i]));
+    }
 
     // errors surface as exceptions (the reference has no error channel)
     bool threw = false;

@@ -112,30 +112,52 @@ __global__ void __launch_bounds__(BLOCK) seg_block_kernel(SegArgs a)
 template <typename C, int TILE>
 __global__ void __launch_bounds__(256) seg_hist_kernel(SegArgs a)
 {
+    // Each CTA takes a contiguous run of tiles.  Tiles of one segment are
+    // contiguous, so the CTA accumulates in shared memory and adds to the
+    // segment's global histograms only when the segment changes (once per
+    // segment it touches, not once per tile).
     __shared__ uint32_t sh[MAX_PASSES * RADIX];
     const int tid = threadIdx.x;
     const int P = a.passes;
+    const uint32_t per = (a.T + gridDim.x - 1) / gridDim.x;
+    const uint32_t t0 = blockIdx.x * per;
+    const uint32_t t1 = min(a.T, t0 + per);
     for (int i = tid; i < P * RADIX; i += 256) sh[i] = 0;
-    const uint32_t t = blockIdx.x;
-    const uint32_t l = a.tile_large[t];
-    const uint32_t s = a.large_ids[l];
-    const uint64_t off = a.offsets[s];
-    const uint32_t len = (uint32_t)(a.offsets[s + 1] - off);
-    const uint32_t base = (t - a.large_tile0[l]) * (uint32_t)TILE;
-    const uint32_t end = min(len, base + (uint32_t)TILE);
-    // the first pass's look-back rows of this tile start cleared
-    for (int i = tid; i < RADIX; i += 256) a.status[(size_t)t * RADIX + i] = 0;
-    __syncthreads();
-    const C *keys = static_cast<const C *>(a.keys) + off;
-    for (uint32_t i = base + tid; i < end; i += 256) {
-        const C c = to_code(keys[i], a.xf);
-        for (int p = 0; p < P; ++p)
-            atomicAdd(&sh[p * RADIX + (uint32_t(c >> (p * RADIX_BITS)) & (RADIX - 1))], 1u);
+    uint32_t cur = 0xffffffffu;   // large-segment index being accumulated
+    auto flush = [&]() {
+        __syncthreads();
+        if (cur != 0xffffffffu) {
+            uint32_t *gh = a.seg_hist + (size_t)cur * P * RADIX;
+            for (int i = tid; i < P * RADIX; i += 256) {
+                if (sh[i]) atomicAdd(&gh[i], sh[i]);
+                sh[i] = 0;
+            }
+        }
+        __syncthreads();
+    };
+    for (uint32_t t = t0; t < t1; ++t) {
+        const uint32_t l = a.tile_large[t];
+        if (l != cur) {
+            flush();
+            cur = l;
+        }
+        const uint32_t s = a.large_ids[l];
+        const uint64_t off = a.offsets[s];
+        const uint32_t len = (uint32_t)(a.offsets[s + 1] - off);
+        const uint32_t base = (t - a.large_tile0[l]) * (uint32_t)TILE;
+        const uint32_t end = min(len, base + (uint32_t)TILE);
+        // the first pass's look-back row of this tile starts cleared
+        for (int i = tid; i < RADIX; i += 256) a.status[(size_t)t * RADIX + i] = 0;
+        const C *keys = static_cast<const C *>(a.keys) + off;
+        for (uint32_t i = base + tid; i < end; i += 256) {
+            const C c = to_code(keys[i], a.xf);
+#pragma unroll
+            for (int p = 0; p < (int)sizeof(C); ++p)
+                if (p < P)
+                    atomicAdd(&sh[p * RADIX + (uint32_t(c >> (p * RADIX_BITS)) & (RADIX - 1))], 1u);
+        }
     }
-    __syncthreads();
-    uint32_t *gh = a.seg_hist + (size_t)l * P * RADIX;
-    for (int i = tid; i < P * RADIX; i += 256)
-        if (sh[i]) atomicAdd(&gh[i], sh[i]);
+    flush();
 }
 
 // ---- large segments: bucket starts (per segment, per pass) -------------------
@@ -406,7 +428,8 @@ static int seg_launch(const SegPlan &p, SegArgs a, cudaStream_t s)
         b.T = (uint32_t)p.tlarge.size();
         XSS_CUDA_TRY(cudaMemsetAsync(b.seg_hist, 0, (size_t)b.L * b.passes * RADIX * 4, s));
         XSS_CUDA_TRY(cudaMemsetAsync(b.tile_ctr, 0, MAX_PASSES * 4, s));
-        XSS_LAUNCH(PK_SEG_MISC, s, (seg_hist_kernel<C, TILE><<<b.T, 256, 0, s>>>(b)));
+        const uint32_t hgrid = (uint32_t)std::max<size_t>(1, std::min<size_t>(b.T, (size_t)num_sms() * 8));
+        XSS_LAUNCH(PK_SEG_MISC, s, (seg_hist_kernel<C, TILE><<<hgrid, 256, 0, s>>>(b)));
         XSS_CUDA_TRY(cudaGetLastError());
         XSS_LAUNCH(PK_SEG_MISC, s, (seg_scan_kernel<<<b.L, 256, 0, s>>>(b)));
         XSS_CUDA_TRY(cudaGetLastError());

@@ -6,14 +6,18 @@
 //   src/xss-common-keyvaluesort.hpp:519-562, 655-738 (kvselect_, select/partial kv)
 //
 // Method: find the exact k-th code by histogramming 11-bit digits from the
-// top (round 0 reads every key; round 1 reads every key again and compacts
-// the keys that share the chosen top digit; later rounds read only those
-// candidates).  With the k-th code K and the counts of codes < K and == K
-// known, the array is partitioned in place: every element whose class
-// (<, ==, > K) does not match the region its position falls in is appended
-// to a per-class list, its position to the per-region hole list, and a
-// second kernel moves list entries into holes.  Only misplaced elements are
-// written, as in an in-place quickselect partition.
+// top.  Round 0 reads every key and picks the bucket B of the top digit that
+// holds rank k: keys below B (class L) belong in [0, b_lo), keys of B in
+// [b_lo, b_lo + b_n), keys above (G) after that.  One more read of every key
+// (the split kernel) does three things at once: it compacts B's keys (with
+// their values or positions) into a candidate list, histograms their next
+// digit for round 1, and records every L or G element that lies outside its
+// region in a per-class list and every L/G-region position holding a
+// foreign element in a per-region hole list.  Later rounds read only the
+// candidates.  With the exact k-th code K known, the candidates are written
+// back into B's region partitioned around K, and a last kernel moves the
+// listed L/G elements into the holes.  Only misplaced elements move, as in
+// an in-place quickselect partition, and the array is read twice.
 #include <algorithm>
 #include <cstring>
 #include <type_traits>
@@ -32,8 +36,11 @@ struct SelState {
     unsigned long long mask;
     unsigned long long cl;
     unsigned long long ce;
+    unsigned long long b_lo;   // keys whose top digit is below the round-0 bucket
+    unsigned long long b_n;    // keys in the round-0 bucket (the candidates)
     unsigned int nmis[3];
     unsigned int nhole[3];
+    unsigned int nbpart[3];    // candidates placed per class (< K, == K, > K)
     unsigned int hist[SEL_BINS];
 };
 
@@ -45,7 +52,8 @@ struct SelArgs {
     KeyXform xf;
     int op;
     SelState *st;
-    void *cand;
+    void *cand;            // candidate codes
+    void *cand_p;          // candidate values (key-value) or positions (argselect)
     void *mis_k;
     void *mis_v;
     uint32_t *holes;
@@ -79,24 +87,10 @@ __device__ __forceinline__ uint32_t sel_block_excl_scan(uint32_t v, uint32_t *s_
     return pre + x - v;
 }
 
-// Warp-aggregated append: returns this lane's slot among lanes with `pred`.
-__device__ __forceinline__ uint32_t warp_append(bool pred, unsigned int *counter)
-{
-    const uint32_t m = __ballot_sync(0xffffffffu, pred);
-    if (m == 0) return 0;
-    const int lane = threadIdx.x & 31;
-    const int leader = __ffs(m) - 1;
-    uint32_t base = 0;
-    if (lane == leader) base = atomicAdd(counter, (unsigned)__popc(m));
-    base = __shfl_sync(0xffffffffu, base, leader);
-    return base + __popc(m & ((1u << lane) - 1u));
-}
-
-// One histogram round over every key (rounds 0, 1) or over the compacted
-// candidates (rounds >= 2).  16-byte vector loads, four per thread in
-// flight, keep enough bytes moving to cover memory latency; an unaligned
-// array takes the scalar loop.  Every loop bound is uniform across a warp so
-// the ballots of the round-1 compaction see all 32 lanes.
+// One histogram round over every key (round 0) or over the compacted
+// candidates (rounds >= 2; round 1 is the split pass).  16-byte vector
+// loads, four per thread in flight, keep enough bytes moving to cover memory
+// latency; an unaligned array takes the scalar loop.
 template <typename C>
 __global__ void __launch_bounds__(256) sel_hist_kernel(SelArgs a, int round, int lo, int bits)
 {
@@ -107,22 +101,17 @@ __global__ void __launch_bounds__(256) sel_hist_kernel(SelArgs a, int round, int
     for (int i = threadIdx.x; i < nb; i += 256) sh[i] = 0;
     __syncthreads();
     const C prefix = (C)a.st->prefix, mask = (C)a.st->mask;
-    const size_t count = round <= 1 ? a.n : (size_t)a.st->cand_n;
-    const C *src = round <= 1 ? static_cast<const C *>(a.keys) : static_cast<const C *>(a.cand);
-    C *cand = static_cast<C *>(a.cand);
+    const size_t count = round == 0 ? a.n : (size_t)a.st->cand_n;
+    const C *src = round == 0 ? static_cast<const C *>(a.keys) : static_cast<const C *>(a.cand);
     const int lane = threadIdx.x & 31;
     const size_t stride = (size_t)gridDim.x * 256;
     const size_t wbase = (size_t)blockIdx.x * 256 + threadIdx.x - lane;   // warp's first thread
 
     auto visit = [&](C b, bool active) {
         C c = 0;
-        if (active) c = round <= 1 ? to_code(b, a.xf) : b;
+        if (active) c = round == 0 ? to_code(b, a.xf) : b;
         const bool match = active && ((C)(c & mask) == prefix);
         if (match) atomicAdd(&sh[uint32_t(c >> lo) & (uint32_t)(nb - 1)], 1u);
-        if (round == 1) {
-            const uint32_t slot = warp_append(match, (unsigned int *)&a.st->cand_n);
-            if (match) cand[slot] = c;
-        }
     };
 
     size_t head = 0;
@@ -178,6 +167,10 @@ __global__ void __launch_bounds__(1024) sel_find_kernel(SelArgs a, int round, in
                 a.st->k_rem = krem - cum;
                 a.st->prefix |= (unsigned long long)b << lo;
                 a.st->mask |= (unsigned long long)(nb - 1) << lo;
+                if (round == 0) {
+                    a.st->b_lo = a.st->cnt_less;
+                    a.st->b_n = h;
+                }
                 if (last) {
                     a.st->cl = a.st->cnt_less;
                     a.st->ce = h;
@@ -192,25 +185,28 @@ __global__ void __launch_bounds__(1024) sel_find_kernel(SelArgs a, int round, in
     if (round == 0 && t == 0) a.st->cand_n = 0;
 }
 
-// Block-wide exclusive scan of three 32-bit words per thread (each word
-// packs two 16-bit counters that cannot overflow within one chunk).
-__device__ __forceinline__ void sel_scan3(uint32_t (&v)[3], uint32_t (*s_w)[3], uint32_t (&tot)[3])
+// Block-wide exclusive scan of NW 32-bit words per thread (each word packs
+// two 16-bit counters that cannot overflow within one chunk); tot = block sums.
+template <int NW>
+__device__ __forceinline__ void sel_scan(uint32_t (&v)[NW], uint32_t (*s_w)[NW], uint32_t (&tot)[NW])
 {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    uint32_t x[3] = {v[0], v[1], v[2]};
+    uint32_t x[NW];
+#pragma unroll
+    for (int q = 0; q < NW; ++q) x[q] = v[q];
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
 #pragma unroll
-        for (int q = 0; q < 3; ++q) {
+        for (int q = 0; q < NW; ++q) {
             const uint32_t y = __shfl_up_sync(0xffffffffu, x[q], o);
             if (lane >= o) x[q] += y;
         }
     }
     if (lane == 31)
-        for (int q = 0; q < 3; ++q) s_w[warp][q] = x[q];
+        for (int q = 0; q < NW; ++q) s_w[warp][q] = x[q];
     __syncthreads();
 #pragma unroll
-    for (int q = 0; q < 3; ++q) {
+    for (int q = 0; q < NW; ++q) {
         uint32_t pre = 0, t = 0;
         for (int w = 0; w < 8; ++w) {
             const uint32_t c = s_w[w][q];
@@ -223,111 +219,135 @@ __device__ __forceinline__ void sel_scan3(uint32_t (&v)[3], uint32_t (*s_w)[3], 
     __syncthreads();
 }
 
-// Partition bookkeeping: every element whose class (<, ==, > K) differs from
-// the region its position lies in goes to its class's list, its position to
-// its region's hole list.  A CTA takes chunks of 256 * IPT elements, each
-// thread IPT consecutive ones (8 16-bit or 32 bytes of wider keys; 16-byte
-// vector loads when the array is aligned), so the lists come out in position
-// order and the placing kernel's writes are coalesced.  Per element the work
-// is 32-bit: region bounds relative to the thread's first element, six list
-// counters in 4-bit fields of one word.  List slots are reserved with one
-// global atomic per list per chunk, and a chunk without misplaced elements
-// skips that step.  The next chunk's keys are loaded before the current
-// chunk's scan, so reads stay in flight across the chunk's barriers.
-template <typename C, typename V>
-__global__ void __launch_bounds__(256) sel_collect_kernel(SelArgs a)
+// Keys per thread per chunk: 8 16-bit keys or 32 bytes of wider keys, read
+// with 16-byte vector loads when the array is aligned.
+template <typename C> struct SelChunk {
+    static constexpr int IPT = sizeof(C) >= 4 ? 32 / (int)sizeof(C) : 8;
+    static constexpr int NV = IPT * (int)sizeof(C) / 16;
+    static constexpr int CH = 256 * IPT;
+};
+
+template <typename C>
+__device__ __forceinline__ void sel_load_chunk(const C *keys, size_t n, size_t p0, bool vec,
+                                               C (&out)[SelChunk<C>::IPT])
 {
-    constexpr int IPT = sizeof(C) >= 4 ? 32 / (int)sizeof(C) : 8, CH = 256 * IPT;
-    constexpr int NV = IPT * (int)sizeof(C) / 16;   // 16-byte vectors per thread
-    __shared__ uint32_t s_w[8][3];
-    __shared__ unsigned long long s_base[6];
-    const C K = (C)a.st->prefix;
-    const size_t cl = a.st->cl, ce = a.st->ce;
+    constexpr int IPT = SelChunk<C>::IPT, NV = SelChunk<C>::NV;
+    if (vec && p0 + IPT <= n) {
+        uint4 q[NV];
+        const uint4 *src = reinterpret_cast<const uint4 *>(keys + p0);
+#pragma unroll
+        for (int v = 0; v < NV; ++v) q[v] = src[v];
+        memcpy(out, q, sizeof(out));
+    } else {
+#pragma unroll
+        for (int j = 0; j < IPT; ++j) out[j] = p0 + j < n ? keys[p0 + j] : C(0);
+    }
+}
+
+// The split pass (see the file comment).  Lists: 0 = L elements outside
+// [0, b_lo), 2 = G elements outside [b_lo + b_n, n), holes 0 / 2 = foreign
+// positions inside those regions, candidates = B's keys.  Each CTA takes
+// chunks of 256 * IPT elements, IPT consecutive ones per thread, so lists
+// come out in position order; slots are reserved with one global atomic per
+// list per chunk (skipped when a chunk has nothing to record), and the next
+// chunk's keys are loaded before the current chunk's scan.  The per-thread
+// counters are 4-bit fields of one word; region tests are 32-bit offsets
+// from the thread's first element.
+template <typename C, typename V>
+__global__ void __launch_bounds__(256) sel_split_kernel(SelArgs a, int lo, int bits)
+{
+    constexpr int IPT = SelChunk<C>::IPT, CH = SelChunk<C>::CH;
+    __shared__ uint32_t s_w[8][4];
+    __shared__ unsigned long long s_base[7];
+    __shared__ uint32_t sh[SEL_BINS];
+    const int tid = threadIdx.x;
+    const int nb = 1 << bits;
+    for (int i = tid; i < nb; i += 256) sh[i] = 0;
+    __syncthreads();
+    const C pre = (C)a.st->prefix, msk = (C)a.st->mask;
+    const size_t b_lo = a.st->b_lo, b_hi = a.st->b_lo + a.st->b_n;
     const C *keys = static_cast<const C *>(a.keys);
     const V *vals = static_cast<const V *>(a.vals);
     C *mis_k = static_cast<C *>(a.mis_k);
     V *mis_v = static_cast<V *>(a.mis_v);
+    C *cand = static_cast<C *>(a.cand);
     const size_t n = a.n;
-    const int tid = threadIdx.x;
     const size_t gstride = (size_t)gridDim.x * CH;
     const bool vec = (reinterpret_cast<uintptr_t>(keys) & 15) == 0;
     C nxt[IPT];
-    auto load_chunk = [&](size_t c0) {
-        const size_t p0 = c0 + (size_t)tid * IPT;
-        if (vec && p0 + IPT <= n) {
-            uint4 q[NV];
-            const uint4 *src = reinterpret_cast<const uint4 *>(keys + p0);
-#pragma unroll
-            for (int v = 0; v < NV; ++v) q[v] = src[v];
-            memcpy(nxt, q, sizeof(nxt));
-        } else {
-#pragma unroll
-            for (int j = 0; j < IPT; ++j) nxt[j] = p0 + j < n ? keys[p0 + j] : C(0);
-        }
-    };
-    load_chunk((size_t)blockIdx.x * CH);
+    sel_load_chunk<C>(keys, n, (size_t)blockIdx.x * CH + (size_t)tid * IPT, vec, nxt);
     for (size_t c0 = (size_t)blockIdx.x * CH; c0 < n; c0 += gstride) {
         C raw[IPT];
 #pragma unroll
         for (int j = 0; j < IPT; ++j) raw[j] = nxt[j];
-        if (c0 + gstride < n) load_chunk(c0 + gstride);
+        if (c0 + gstride < n) sel_load_chunk<C>(keys, n, c0 + gstride + (size_t)tid * IPT, vec, nxt);
         const size_t p0 = c0 + (size_t)tid * IPT;
-        // region boundaries relative to this thread's first element, clamped
-        // to [0, IPT], so the per-element region test is 32-bit
-        const uint32_t r1 = (uint32_t)(cl > p0 ? min(cl - p0, (size_t)IPT) : 0);
-        const uint32_t r2 = (uint32_t)(cl + ce > p0 ? min(cl + ce - p0, (size_t)IPT) : 0);
+        const uint32_t r1 = (uint32_t)(b_lo > p0 ? min(b_lo - p0, (size_t)IPT) : 0);
+        const uint32_t r2 = (uint32_t)(b_hi > p0 ? min(b_hi - p0, (size_t)IPT) : 0);
         const uint32_t valid = (uint32_t)(n > p0 ? min(n - p0, (size_t)IPT) : 0);
-        uint32_t tags = 0;                      // 4 bits per element: list class, hole region
-        uint32_t cnt4 = 0;                      // 4-bit counters: lists 0..2, holes 0..2
+        uint32_t tags = 0;      // 4 bits per element: list class (0, 2 or 3 = none), hole region
+        uint32_t candm = 0;     // bit j: element j is a candidate
+        uint32_t cnt4 = 0;      // 4-bit counters: lists 0..2, holes 0..2, candidates
 #pragma unroll
         for (int j = 0; j < IPT; ++j) {
             uint32_t t = 0xF;
             if ((uint32_t)j < valid) {
                 const C c = to_code(raw[j], a.xf);
-                const uint32_t cls = (uint32_t)(c >= K) + (uint32_t)(c > K);
+                const C top = (C)(c & msk);
+                const uint32_t cls = (uint32_t)(top >= pre) + (uint32_t)(top > pre);
                 const uint32_t reg = (uint32_t)((uint32_t)j >= r1) + (uint32_t)((uint32_t)j >= r2);
-                if (a.op == SOP_ARG) a.out_idx[p0 + j] = p0 + j;
+                if (a.op == SOP_ARG && reg != 1) a.out_idx[p0 + j] = p0 + j;
+                if (cls == 1) {
+                    candm |= 1u << j;
+                    cnt4 += 1u << 24;
+                    atomicAdd(&sh[uint32_t(c >> lo) & (uint32_t)(nb - 1)], 1u);
+                }
                 if (cls != reg) {
-                    const bool rec = a.op != SOP_KEYS || cls != 1;
-                    t = (rec ? cls : 3u) | (reg << 2);
-                    cnt4 += (rec ? (1u << (4 * cls)) : 0u) + (1u << (4 * (3 + reg)));
+                    const uint32_t X = cls == 1 ? 3u : cls;   // candidates are not listed
+                    const uint32_t R = reg == 1 ? 3u : reg;   // B's region is rewritten whole
+                    t = X | (R << 2);
+                    cnt4 += (X != 3u ? (1u << (4 * X)) : 0u) + (R != 3u ? (1u << (4 * (3 + R))) : 0u);
                 }
             }
             tags |= t << (4 * j);
         }
         if (!__syncthreads_or(cnt4 != 0u)) continue;
-        // two 16-bit counters per scanned word
-        uint32_t w[3];
+        uint32_t w[4];
 #pragma unroll
         for (int q = 0; q < 3; ++q)
             w[q] = ((cnt4 >> (8 * q)) & 0xFu) | (((cnt4 >> (8 * q + 4)) & 0xFu) << 16);
-        uint32_t tot[3];
-        sel_scan3(w, s_w, tot);
-        if (tid < 6) {
-            const uint32_t t = (tot[tid >> 1] >> ((tid & 1) * 16)) & 0xFFFFu;
-            unsigned int *ctr = tid < 3 ? &a.st->nmis[tid] : &a.st->nhole[tid - 3];
-            const size_t rs = (tid % 3) == 0 ? 0 : ((tid % 3) == 1 ? cl : cl + ce);
+        w[3] = (cnt4 >> 24) & 0xFu;
+        uint32_t tot[4];
+        sel_scan<4>(w, s_w, tot);
+        if (tid < 7) {
+            const uint32_t t = tid < 6 ? (tot[tid >> 1] >> ((tid & 1) * 16)) & 0xFFFFu : tot[3];
+            unsigned long long *ctr64 = nullptr;
+            unsigned int *ctr = nullptr;
+            if (tid < 3) ctr = &a.st->nmis[tid];
+            else if (tid < 6) ctr = &a.st->nhole[tid - 3];
+            else ctr64 = &a.st->cand_n;
+            const size_t rs = tid == 6 ? 0 : ((tid % 3) == 0 ? 0 : ((tid % 3) == 1 ? b_lo : b_hi));
+            size_t at = rs;
+            if (t) at += ctr ? (size_t)atomicAdd(ctr, t) : (size_t)atomicAdd(ctr64, (unsigned long long)t);
             // a list that would run past the array (never, with consistent
             // counts) is not written for this chunk
-            const size_t at = rs + (t ? atomicAdd(ctr, t) : 0u);
             s_base[tid] = at + t <= n ? at : ~0ull;
         }
         __syncthreads();
-        // this thread's first slot in each list: chunk base + exclusive prefix
-        size_t slot[6];
-        bool ok[6];
+        size_t slot[7];
+        bool ok[7];
 #pragma unroll
-        for (int q = 0; q < 6; ++q) {
+        for (int q = 0; q < 7; ++q) {
             const unsigned long long b0 = s_base[q];
             ok[q] = b0 != ~0ull;
-            slot[q] = b0 + ((w[q >> 1] >> ((q & 1) * 16)) & 0xFFFFu);
+            slot[q] = b0 + (q < 6 ? ((w[q >> 1] >> ((q & 1) * 16)) & 0xFFFFu) : w[3]);
         }
 #pragma unroll
         for (int j = 0; j < IPT; ++j) {
             const size_t p = p0 + j;
             const uint32_t X = (tags >> (4 * j)) & 3u, R = (tags >> (4 * j + 2)) & 3u;
 #pragma unroll
-            for (int q = 0; q < 3; ++q) {
+            for (int q = 0; q < 3; q += 2) {
                 if (X == (uint32_t)q) {
                     if (ok[q]) {
                         const size_t at = slot[q];
@@ -346,27 +366,115 @@ __global__ void __launch_bounds__(256) sel_collect_kernel(SelArgs a)
                     ++slot[3 + q];
                 }
             }
+            if ((candm >> j) & 1u) {
+                if (ok[6]) {
+                    const size_t at = slot[6];
+                    cand[at] = to_code(raw[j], a.xf);
+                    if (a.op == SOP_ARG) {
+                        static_cast<uint32_t *>(a.cand_p)[at] = (uint32_t)p;
+                    } else if constexpr (!std::is_same<V, uint8_t>::value) {
+                        if (a.op == SOP_KV) static_cast<V *>(a.cand_p)[at] = vals[p];
+                    }
+                }
+                ++slot[6];
+            }
+        }
+        __syncthreads();   // s_base is rewritten by the next chunk
+    }
+    for (int i = tid; i < nb; i += 256)
+        if (sh[i]) atomicAdd(&a.st->hist[i], sh[i]);
+}
+
+// B's region rewritten from the candidates, partitioned around K:
+// [b_lo, cl) < K, [cl, cl + ce) == K, [cl + ce, b_lo + b_n) > K.  Same chunk
+// and slot reservation scheme as the split pass, over the candidate list.
+template <typename C, typename V>
+__global__ void __launch_bounds__(256) sel_bpart_kernel(SelArgs a)
+{
+    constexpr int IPT = SelChunk<C>::IPT, CH = SelChunk<C>::CH;
+    __shared__ uint32_t s_w[8][2];
+    __shared__ unsigned long long s_base[3];
+    const int tid = threadIdx.x;
+    const C K = (C)a.st->prefix;
+    const size_t cl = a.st->cl, ce = a.st->ce;
+    const size_t b_lo = a.st->b_lo, b_n = a.st->b_n;
+    const size_t m = min((size_t)a.st->cand_n, b_n);
+    const size_t rstart[3] = {b_lo, cl, cl + ce};
+    const size_t rend[3] = {cl, cl + ce, b_lo + b_n};
+    const C *cand = static_cast<const C *>(a.cand);
+    C *keys = static_cast<C *>(a.keys);
+    V *vals = static_cast<V *>(a.vals);
+    for (size_t c0 = (size_t)blockIdx.x * CH; c0 < m; c0 += (size_t)gridDim.x * CH) {
+        const size_t p0 = c0 + (size_t)tid * IPT;
+        const uint32_t valid = (uint32_t)(m > p0 ? min(m - p0, (size_t)IPT) : 0);
+        C cc[IPT];
+        uint32_t cls4 = 0, cnt4 = 0;
+#pragma unroll
+        for (int j = 0; j < IPT; ++j) {
+            cc[j] = (uint32_t)j < valid ? cand[p0 + j] : C(0);
+            const uint32_t cls = (uint32_t)(cc[j] >= K) + (uint32_t)(cc[j] > K);
+            if ((uint32_t)j < valid) {
+                cls4 |= cls << (2 * j);
+                cnt4 += 1u << (4 * cls);
+            }
+        }
+        uint32_t w[2] = {(cnt4 & 0xFu) | (((cnt4 >> 4) & 0xFu) << 16), (cnt4 >> 8) & 0xFu};
+        uint32_t tot[2];
+        sel_scan<2>(w, s_w, tot);
+        if (tid < 3) {
+            const uint32_t t = tid < 2 ? (tot[0] >> (16 * tid)) & 0xFFFFu : tot[1];
+            const size_t at = rstart[tid] + (t ? atomicAdd(&a.st->nbpart[tid], t) : 0u);
+            s_base[tid] = at + t <= rend[tid] ? at : ~0ull;
+        }
+        __syncthreads();
+        size_t slot[3];
+        bool ok[3];
+#pragma unroll
+        for (int q = 0; q < 3; ++q) {
+            ok[q] = s_base[q] != ~0ull;
+            slot[q] = s_base[q] + (q < 2 ? (w[0] >> (16 * q)) & 0xFFFFu : w[1]);
+        }
+#pragma unroll
+        for (int j = 0; j < IPT; ++j) {
+            if ((uint32_t)j >= valid) continue;
+            const uint32_t cls = (cls4 >> (2 * j)) & 3u;
+#pragma unroll
+            for (int q = 0; q < 3; ++q) {
+                if (cls == (uint32_t)q) {
+                    if (ok[q] && slot[q] < a.n) {
+                        const size_t at = slot[q];
+                        if (a.op == SOP_ARG) {
+                            a.out_idx[at] = static_cast<const uint32_t *>(a.cand_p)[p0 + j];
+                        } else {
+                            keys[at] = from_code(cc[j], a.xf);
+                            if constexpr (!std::is_same<V, uint8_t>::value)
+                                if (a.op == SOP_KV) vals[at] = static_cast<const V *>(a.cand_p)[p0 + j];
+                        }
+                    }
+                    ++slot[q];
+                }
+            }
         }
         __syncthreads();   // s_base is rewritten by the next chunk
     }
 }
 
+// Listed L / G elements into the holes of their regions.
 template <typename C, typename V>
 __global__ void __launch_bounds__(256) sel_place_kernel(SelArgs a)
 {
-    const C K = (C)a.st->prefix;
-    const size_t cl = a.st->cl, ce = a.st->ce;
-    const size_t regstart[3] = {0, cl, cl + ce};
+    const size_t b_lo = a.st->b_lo, b_hi = a.st->b_lo + a.st->b_n;
     C *keys = static_cast<C *>(a.keys);
     V *vals = static_cast<V *>(a.vals);
     const C *mis_k = static_cast<const C *>(a.mis_k);
     const V *mis_v = static_cast<const V *>(a.mis_v);
-    const C kraw = from_code(K, a.xf);
     const size_t stride = (size_t)gridDim.x * 256;
-    for (int X = 0; X < 3; ++X) {
+#pragma unroll
+    for (int X = 0; X < 3; X += 2) {
+        const size_t rs = X == 0 ? 0 : b_hi;
         // counts are consistent by construction; clamp so a broken state can
         // never index past the lists
-        const size_t cnt = min((size_t)a.st->nhole[X], a.n - regstart[X]);
+        const size_t cnt = min((size_t)a.st->nhole[X], a.n - min(rs, a.n));
         // four list entries per thread in flight
         constexpr int U = 4;
         for (size_t j0 = (size_t)blockIdx.x * 256 + threadIdx.x; j0 < cnt; j0 += U * stride) {
@@ -375,30 +483,29 @@ __global__ void __launch_bounds__(256) sel_place_kernel(SelArgs a)
 #pragma unroll
             for (int u = 0; u < U; ++u) {
                 const size_t j = j0 + u * stride;
-                pos[u] = j < cnt ? a.holes[regstart[X] + j] : 0xffffffffu;
-                mk[u] = (j < cnt && a.op == SOP_KEYS && X != 1) ? mis_k[regstart[X] + j] : C(0);
+                pos[u] = j < cnt ? a.holes[rs + j] : 0xffffffffu;
+                mk[u] = (j < cnt && a.op != SOP_ARG) ? mis_k[rs + j] : C(0);
             }
 #pragma unroll
             for (int u = 0; u < U; ++u) {
                 const size_t j = j0 + u * stride;
                 if (j >= cnt || pos[u] >= a.n) continue;
-                const size_t at = regstart[X] + j;
+                const size_t at = rs + j;
                 if (a.op == SOP_ARG) {
                     a.out_idx[pos[u]] = reinterpret_cast<const uint32_t *>(a.mis_v)[at];
-                } else if (a.op == SOP_KEYS) {
-                    keys[pos[u]] = X == 1 ? kraw : mk[u];
                 } else {
-                    keys[pos[u]] = mis_k[at];
+                    keys[pos[u]] = mk[u];
                     if constexpr (!std::is_same<V, uint8_t>::value)
                         if (a.op == SOP_KV) vals[pos[u]] = mis_v[at];
                 }
             }
         }
     }
+    (void)b_lo;
 }
 
 struct SelLayout {
-    size_t st, cand, mis_k, mis_v, holes, total;
+    size_t st, cand, cand_p, mis_k, mis_v, holes, total;
 };
 
 static SelLayout sel_layout(int op, int kbytes, int vbytes, size_t n)
@@ -408,6 +515,7 @@ static SelLayout sel_layout(int op, int kbytes, int vbytes, size_t n)
     size_t off = 0;
     L.st = off;    off = align_up(off + sizeof(SelState), 256);
     L.cand = off;  off = align_up(off + n * kbytes, 256);
+    L.cand_p = off; if (vb) off = align_up(off + n * vb, 256);
     L.mis_k = off; if (op != SOP_ARG) off = align_up(off + n * kbytes, 256);
     L.mis_v = off; if (vb) off = align_up(off + n * vb, 256);
     L.holes = off; off = align_up(off + n * 4, 256);
@@ -438,6 +546,7 @@ static int select_launch(int op, KeyXform xf, void *keys, void *vals, uint64_t *
     a.op = op;
     a.st = reinterpret_cast<SelState *>(base + L.st);
     a.cand = base + L.cand;
+    a.cand_p = base + L.cand_p;
     a.mis_k = base + L.mis_k;
     a.mis_v = base + L.mis_v;
     a.holes = reinterpret_cast<uint32_t *>(base + L.holes);
@@ -446,23 +555,29 @@ static int select_launch(int op, KeyXform xf, void *keys, void *vals, uint64_t *
     const int sms = num_sms();
     const int grid = (int)std::max<size_t>(1, std::min<size_t>((n + 2047) / 2048, (size_t)sms * 8));
     const int W = 8 * (int)sizeof(C);
-    const int rounds = (W + SEL_DIGIT - 1) / SEL_DIGIT;
+    const int rounds = (W + SEL_DIGIT - 1) / SEL_DIGIT;   // >= 2 for every key width
     for (int r = 0; r < rounds; ++r) {
         const int hi = W - SEL_DIGIT * r;
         const int lo = std::max(0, hi - SEL_DIGIT);
         const int bits = hi - lo;
-        // rounds >= 2 scan only the compacted candidates; a smaller grid does
-        const int g = r >= 2 ? std::max(1, grid / 4) : grid;
-        XSS_LAUNCH(PK_SEL_HIST, s, sel_hist_kernel<C><<<g, 256, 0, s>>>(a, r, lo, bits));
+        if (r == 1) {
+            // one read of every key: candidates, their next-digit histogram,
+            // and the L / G lists and holes
+            XSS_LAUNCH(PK_SEL_COLLECT, s, (sel_split_kernel<C, V><<<grid, 256, 0, s>>>(a, lo, bits)));
+        } else {
+            // round 0 reads every key; later rounds only the candidates
+            const int g = r >= 2 ? std::max(1, grid / 4) : grid;
+            XSS_LAUNCH(PK_SEL_HIST, s, sel_hist_kernel<C><<<g, 256, 0, s>>>(a, r, lo, bits));
+        }
         XSS_CUDA_TRY(cudaGetLastError());
         XSS_LAUNCH(PK_SEL_FIND, s,
                    sel_find_kernel<C><<<1, 1024, 0, s>>>(a, r, lo, bits, r == rounds - 1,
                                                          (unsigned long long)k));
         XSS_CUDA_TRY(cudaGetLastError());
     }
-    XSS_LAUNCH(PK_SEL_COLLECT, s, sel_collect_kernel<C, V><<<grid, 256, 0, s>>>(a));
+    XSS_LAUNCH(PK_SEL_PLACE, s, (sel_bpart_kernel<C, V><<<grid, 256, 0, s>>>(a)));
     XSS_CUDA_TRY(cudaGetLastError());
-    XSS_LAUNCH(PK_SEL_PLACE, s, sel_place_kernel<C, V><<<grid, 256, 0, s>>>(a));
+    XSS_LAUNCH(PK_SEL_PLACE, s, (sel_place_kernel<C, V><<<grid, 256, 0, s>>>(a)));
     XSS_CUDA_TRY(cudaGetLastError());
     return XSS_OK;
 }
