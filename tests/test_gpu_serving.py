@@ -123,3 +123,34 @@ def test_full_queue_sheds_and_shutdown_drains(xss, cuda):
     want = np.sort(x)
     for _, xo in tickets:
         assert np.array_equal(xo, want)
+
+
+def test_large_requests_use_shared_sm_lines(xss, cuda):
+    """Above 2^24 keys a sort normally takes the large-array pass lines; the
+    server's thread takes the mid-size lines for every size, with workspace
+    sized for either.  Large requests through the server must match the same
+    sorts done directly."""
+    torch = cuda
+    n = (1 << 24) + 4097
+    rng = np.random.default_rng(31)
+    srv = xss.Server(hbm_budget_bytes=4 << 30, small_max=8192)
+    x = rng.standard_normal(n).astype(np.float32)
+    k64 = rng.integers(np.iinfo(np.int64).min, np.iinfo(np.int64).max, n, dtype=np.int64)
+    v64 = np.arange(n, dtype=np.uint64)
+    bufs = []
+    tin, xin = _pinned(torch, x)
+    tout, xout = _pinned(torch, np.zeros_like(x))
+    tk, kin = _pinned(torch, k64)
+    tko, kout = _pinned(torch, np.zeros_like(k64))
+    tv, vin = _pinned(torch, v64)
+    tvo, vout = _pinned(torch, np.zeros_like(v64))
+    bufs += [tin, tout, tk, tko, tv, tvo]
+    t1 = srv.submit("qsort", "float32", xin.ctypes.data, xout.ctypes.data, n=n)
+    t2 = srv.submit("keyvalue_qsort", "int64", kin.ctypes.data, kout.ctypes.data,
+                    vals_in=vin.ctypes.data, vals_out=vout.ctypes.data, val_dtype="uint64", n=n)
+    assert t1 is not None and t2 is not None
+    assert srv.wait(t1) == 0 and srv.wait(t2) == 0
+    srv.close()
+    assert np.array_equal(xout, np.sort(x))
+    assert np.array_equal(kout, np.sort(k64))
+    assert np.array_equal(k64[vout.astype(np.int64)], kout)

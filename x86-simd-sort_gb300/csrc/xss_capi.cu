@@ -64,6 +64,23 @@ unsigned *device_error_word()
     return g_err[d];
 }
 
+int set_max_dyn_smem(const void *kernel, size_t bytes)
+{
+    static std::mutex mu;
+    static std::map<std::pair<const void *, int>, size_t> done;
+    const int d = cur_device();
+    std::lock_guard<std::mutex> lk(mu);
+    size_t &have = done[std::make_pair(kernel, d)];
+    if (have >= bytes) return XSS_OK;
+    if (cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes) !=
+        cudaSuccess) {
+        cudaGetLastError();
+        return XSS_ECUDA;
+    }
+    have = bytes;
+    return XSS_OK;
+}
+
 int num_sms()
 {
     const int d = cur_device();

@@ -86,6 +86,10 @@ int radix_select(int op, int kbytes, KeyXform xf, void *keys, void *vals, int vb
 
 int num_sms();
 
+// Raise a kernel's dynamic shared-memory limit to `bytes`, once per (kernel,
+// device); thread-safe.  Returns XSS_OK or XSS_ECUDA.
+int set_max_dyn_smem(const void *kernel, size_t bytes);
+
 // Per host thread: sort arrays of every size with the mid-size pass lines
 // (several CTAs per SM), so kernels of concurrent requests on other streams
 // share the SMs.  The serving loop's scheduler thread sets it.

@@ -10,6 +10,7 @@
 // The reference's quicksort is in-place and unstable; an LSD radix sort is
 // stable per pass and yields one of the orders the reference may produce.
 #include <algorithm>
+#include <atomic>
 #include <cstdlib>
 #include <cstring>
 #include <mutex>
@@ -286,13 +287,15 @@ static int resident_passes(const RadixArgs &a, int sms, cudaStream_t s, const La
     constexpr bool HAS_V = !std::is_same<V, NoVal>::value;
     const size_t smem = (PF ? 2 : 1) * TILE * (sizeof(C) + (HAS_V ? sizeof(V) : 0));
     auto kern = onesweep_persist_kernel<C, V, BLOCK, ITEMS, MINB, LB, RANK, DPT, PF>;
-    static int per_sm = 0;
+    int rc = set_max_dyn_smem((const void *)kern, smem);
+    if (rc) return rc;
+    static std::atomic<int> per_sm_cached{0};   // same GPU model on every device
+    int per_sm = per_sm_cached.load(std::memory_order_relaxed);
     if (!per_sm) {
-        XSS_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                          (int)smem));
         int v = 0;
         XSS_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, kern, BLOCK, smem));
         per_sm = std::max(v, 1);
+        per_sm_cached.store(per_sm, std::memory_order_relaxed);
     }
     const uint32_t grid = (uint32_t)std::min<size_t>(a.num_tiles, (size_t)per_sm * sms);
     for (int p = 0; p < a.passes; ++p) {
@@ -310,12 +313,8 @@ static int tile_passes(const RadixArgs &a, cudaStream_t s, const LaunchOpts &o)
     constexpr bool HAS_V = !std::is_same<V, NoVal>::value;
     const size_t smem = TILE * (sizeof(C) + (HAS_V ? sizeof(V) : 0));
     auto kern = onesweep_kernel<C, V, BLOCK, ITEMS, MINB, LB, RANK, DPT>;
-    static bool attr_set = false;
-    if (!attr_set) {
-        XSS_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                          (int)smem));
-        attr_set = true;
-    }
+    const int rc = set_max_dyn_smem((const void *)kern, smem);
+    if (rc) return rc;
     for (int p = 0; p < a.passes; ++p) {
         XSS_LAUNCH_OPT(o, PK_ONESWEEP, s, kern<<<a.num_tiles, BLOCK, smem, s>>>(a, p));
         XSS_CUDA_TRY(cudaGetLastError());
@@ -364,11 +363,9 @@ static int onesweep_launch_cls(int op, KeyXform xf, void *keys, void *vals, uint
     const size_t want = (n + 256 * 16 - 1) / (256 * 16);
     const int hist_grid = (int)std::max<size_t>(1, std::min<size_t>(want, (size_t)sms * 8));
     constexpr size_t HSMEM = hist_smem_bytes<C>();
-    static bool hist_attr = false;
-    if (!hist_attr) {
-        XSS_CUDA_TRY(cudaFuncSetAttribute(hist_kernel<C>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                          (int)HSMEM));
-        hist_attr = true;
+    {
+        const int rc = set_max_dyn_smem((const void *)hist_kernel<C>, HSMEM);
+        if (rc) return rc;
     }
     XSS_LAUNCH_OPT(o, PK_HIST, s, hist_kernel<C><<<hist_grid, 256, HSMEM, s>>>(a));
     XSS_CUDA_TRY(cudaGetLastError());

@@ -435,11 +435,9 @@ static int seg_launch(const SegPlan &p, SegArgs a, cudaStream_t s)
         XSS_CUDA_TRY(cudaGetLastError());
         const size_t smem = TILE * (sizeof(C) + (HAS_V ? sizeof(V) : 0));
         auto kern = seg_pass_kernel<C, V, BLOCK, ITEMS, MINB, LB, RANK, DPT>;
-        static bool attr = false;
-        if (!attr) {
-            XSS_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                              (int)smem));
-            attr = true;
+        {
+            const int rc = set_max_dyn_smem((const void *)kern, smem);
+            if (rc) return rc;
         }
         for (int pass = 0; pass < b.passes; ++pass) {
             XSS_LAUNCH(PK_ONESWEEP, s, (kern<<<b.T, BLOCK, smem, s>>>(b, pass)));
