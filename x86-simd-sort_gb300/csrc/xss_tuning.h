@@ -1,6 +1,9 @@
 // xss_tuning.h -- onesweep pass lines chosen by autotune.py (n = 268435456, _MID classes n = 2097152; uniform keys; median time).
 // Each line: BLOCK, ITEMS, MINB, LB, RANK, PERSIST, DPT.
 #pragma once
+// Look-back width re-measured afterwards (autotune.py --candidates): LB 8 beat LB 16 for
+// K32 (4.255 vs 4.331 ms), K64V64 (17.33 vs 17.49 ms) and DEFAULT (15.23 vs 15.35 ms);
+// those three lines use it.
 
 // K16: 320,20,3,16,0,1,0 2.153 ms; 256,24,3,16,0,1,0 2.273 ms; 512,16,2,16,0,1,0 2.252 ms
 #ifndef XSS_CFG_K16
@@ -9,7 +12,7 @@
 
 // K32: 320,20,3,16,0,1,0 4.389 ms; 256,24,3,16,0,1,0 4.605 ms; 512,16,2,16,0,1,0 4.532 ms; 320,24,2,16,0,1,0 4.816 ms
 #ifndef XSS_CFG_K32
-#define XSS_CFG_K32 320, 20, 3, 16, 0, 1, 0
+#define XSS_CFG_K32 320, 20, 3, 8, 0, 1, 0
 #endif
 
 // K64: 512,16,1,16,0,1,1 12.669 ms; 512,12,1,16,0,1,1 13.474 ms; 256,16,2,16,0,1,0 13.229 ms
@@ -24,12 +27,12 @@
 
 // K64V64: 512,11,1,16,1,1,1 17.939 ms; 512,11,1,16,0,1,1 17.538 ms; 512,10,1,16,0,1,1 18.100 ms; 512,12,1,16,0,1,1 inf ms
 #ifndef XSS_CFG_K64V64
-#define XSS_CFG_K64V64 512, 11, 1, 16, 0, 1, 1
+#define XSS_CFG_K64V64 512, 11, 1, 8, 0, 1, 1
 #endif
 
 // DEFAULT: 512,14,1,16,0,1,1 15.387 ms; 512,12,1,16,0,1,1 15.975 ms; 512,14,1,16,1,1,1 17.137 ms
 #ifndef XSS_CFG_DEFAULT
-#define XSS_CFG_DEFAULT 512, 14, 1, 16, 0, 1, 1
+#define XSS_CFG_DEFAULT 512, 14, 1, 8, 0, 1, 1
 #endif
 
 // K16_MID: 512,16,2,16,0,1,0 0.057 ms; 256,16,3,16,0,1,0 0.060 ms
