@@ -55,7 +55,7 @@ def _peaks():
 # dominant kernel at the workload's full size: one ncu capture of a smaller case
 # scaled by the keys per launch (profiles/onesweep_kv_i64u64_2e25.md x8,
 # profiles/onesweep_f32_2e26.md x4).
-TRAFFIC = {"keyvalue_qsort": 8245047296, "qsort_f32": 1991735296}
+TRAFFIC = {"keyvalue_qsort": 8245616640, "qsort_f32": 1991095296}
 
 
 def _traffic(workload, n, n_full):

@@ -463,7 +463,7 @@ __global__ void __launch_bounds__(256) sel_bpart_kernel(SelArgs a)
 template <typename C, typename V>
 __global__ void __launch_bounds__(256) sel_place_kernel(SelArgs a)
 {
-    const size_t b_lo = a.st->b_lo, b_hi = a.st->b_lo + a.st->b_n;
+    const size_t b_hi = a.st->b_lo + a.st->b_n;
     C *keys = static_cast<C *>(a.keys);
     V *vals = static_cast<V *>(a.vals);
     const C *mis_k = static_cast<const C *>(a.mis_k);
@@ -501,7 +501,6 @@ __global__ void __launch_bounds__(256) sel_place_kernel(SelArgs a)
             }
         }
     }
-    (void)b_lo;
 }
 
 struct SelLayout {
