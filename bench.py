@@ -279,7 +279,7 @@ class SegmentedSort(Workload):
     given total (e.g. 2^27)."""
 
     name = "segmented_sort"
-    kb, vb = 4, 4
+    kdt, kid, kb, vb = "int32", 4, 4, 4
 
     def __init__(self, torch, xss, n, stream):
         super().__init__(torch, xss, n, stream)
@@ -293,16 +293,20 @@ class SegmentedSort(Workload):
         self.n = int(self.off[-1])
 
     def describe(self):
+        keys = "int32 keys uniform full range" if self.kdt == "int32" else "float32 keys N(0,1)"
         return {"workload": f"segmented keyvalue sort, {self.sizes.size} segments, sizes "
-                            f"log-uniform [1, 2^18] (seed 3), int32 keys -> uint32 local index",
+                            f"log-uniform [1, 2^18] (seed 3), {keys} -> uint32 local index",
                 "n": self.n, "segments": int(self.sizes.size),
                 "l2": "inputs far larger than L2; input restored per step"}
 
     def setup(self):
         t, n = self.torch, self.n
         g = t.Generator(device="cuda").manual_seed(3)
-        self.k0 = t.randint(0, 256, (n * 4,), dtype=t.uint8, device="cuda",
-                            generator=g).view(t.int32)
+        if self.kdt == "int32":
+            self.k0 = t.randint(0, 256, (n * 4,), dtype=t.uint8, device="cuda",
+                                generator=g).view(t.int32)
+        else:
+            self.k0 = t.randn(n, dtype=t.float32, device="cuda", generator=g)
         self.doff = t.from_numpy(self.off.view(np.int64).copy()).cuda()
         self.v0 = t.empty(n, dtype=t.int32, device="cuda")
         chunk = 1 << 27
@@ -313,7 +317,7 @@ class SegmentedSort(Workload):
             del idx, seg
         self.k = t.empty_like(self.k0)
         self.v = t.empty_like(self.v0)
-        self.plan = self.xss.SegPlan("int32", "uint32", self.off)
+        self.plan = self.xss.SegPlan(self.kdt, "uint32", self.off)
         self.wsb = self.plan.workspace_size
         self.ws = t.empty(max(self.wsb, 1), dtype=t.uint8, device="cuda")
 
@@ -330,7 +334,7 @@ class SegmentedSort(Workload):
                       self.ws.data_ptr(), self.wsb, self.stream.cuda_stream, use_graph=False)
 
     def run_percall(self):
-        self.xss.gpu_segmented_sort_percall("int32", "uint32", self.k.data_ptr(),
+        self.xss.gpu_segmented_sort_percall(self.kdt, "uint32", self.k.data_ptr(),
                                             self.v.data_ptr(), self.off,
                                             stream=self.stream.cuda_stream)
 
@@ -367,7 +371,10 @@ class SegmentedSort(Workload):
         m = self._cpu_m
         stop = int(np.searchsorted(self.off, m))
         rng = np.random.default_rng(3)
-        k = rng.integers(-2**31, 2**31 - 1, int(self.off[stop]), dtype=np.int32)
+        if self.kdt == "int32":
+            k = rng.integers(-2**31, 2**31 - 1, int(self.off[stop]), dtype=np.int32)
+        else:
+            k = rng.standard_normal(int(self.off[stop])).astype(np.float32)
         v = np.zeros(k.size, np.uint32)
         for s in range(stop):
             b, e = int(self.off[s]), int(self.off[s + 1])
@@ -377,10 +384,11 @@ class SegmentedSort(Workload):
             if e - b <= 1:
                 continue
             if kind == "reference" or e - b <= 10000:
-                rc = lib.keyvalue_qsort(4, 3, k[b:].ctypes.data, v[b:].ctypes.data, e - b, 0, 0)
+                rc = lib.keyvalue_qsort(self.kid, 3, k[b:].ctypes.data, v[b:].ctypes.data, e - b,
+                                        0, 0)
             else:   # the reference's key-value sort goes task-parallel above 1e4 keys
-                rc = lib.keyvalue_qsort_mt(4, 3, k[b:].ctypes.data, v[b:].ctypes.data, e - b, 0,
-                                           0, threads)
+                rc = lib.keyvalue_qsort_mt(self.kid, 3, k[b:].ctypes.data, v[b:].ctypes.data,
+                                           e - b, 0, 0, threads)
             assert rc == 0
         return int(self.off[stop])
 
@@ -509,6 +517,8 @@ class SelectWorkload(Workload):
     name = "qselect_f32"
     dominant = None
     partial = False
+    kb = 4
+    default_k = 1 << 26
 
     def describe(self):
         return {"workload": f"{'partial_qsort' if self.partial else 'qselect'} float32 "
@@ -549,9 +559,9 @@ class SelectWorkload(Workload):
         return None
 
     def bytes_model(self):           # histogram + one partition R+W (+ sort of the top k)
-        m = 3 * self.n * 4
+        m = 3 * self.n * self.kb
         if self.partial:
-            m += self.k * 4 * (1 + 2 * 4)
+            m += self.k * self.kb * (1 + 2 * self.kb)
         return m
 
     def host_setup(self):
@@ -582,15 +592,378 @@ class PartialWorkload(SelectWorkload):
     partial = True
 
 
+
+def zipf16_codes(rng, dtype):
+    """4096 distinct 16-bit patterns; finite values other than -0.0 for float16."""
+    if dtype == "uint16":
+        return rng.choice(65536, 4096, replace=False).astype(np.uint16)
+    pool = np.arange(65536, dtype=np.uint16)
+    finite = pool[((pool & 0x7C00) != 0x7C00) & (pool != 0x8000)]
+    return rng.choice(finite, 4096, replace=False).astype(np.uint16)
+
+
+ZIPF_P = 1.0 / np.arange(1, 4097) ** 1.1
+ZIPF_P /= ZIPF_P.sum()
+
+
+class SelectZipf16(SelectWorkload):
+    """qselect of 2^28 16-bit keys drawn Zipf(s=1.1) over 4096 distinct values
+    (heavy duplicates), k = 2^20 (seed 2)."""
+
+    name = "qselect_u16_zipf"
+    kdt, kid, kb = "uint16", 0, 2
+    default_k = 1 << 20
+
+    def describe(self):
+        return {"workload": f"qselect {self.kdt} n=2^{self.n.bit_length() - 1} Zipf(s=1.1) "
+                            f"over 4096 distinct values k={self.k}",
+                "n": self.n, "k": self.k, "l2": "inputs larger than L2; restored per step"}
+
+    def setup(self):
+        t = self.torch
+        table = t.tensor(zipf16_codes(np.random.default_rng(2), self.kdt).view(np.int16),
+                         device="cuda")
+        cdf = t.tensor(np.cumsum(ZIPF_P), device="cuda")
+        g = t.Generator(device="cuda").manual_seed(2)
+        self.k0 = t.empty(self.n, dtype=t.int16, device="cuda")
+        chunk = 1 << 26
+        for b in range(0, self.n, chunk):
+            m = min(chunk, self.n - b)
+            r = t.searchsorted(cdf, t.rand(m, dtype=t.float64, device="cuda", generator=g))
+            self.k0[b:b + m] = table[r.clamp(max=4095)]
+            del r
+        self.x = t.empty_like(self.k0)
+        self.wsb = self.xss.workspace_size("qselect", self.kdt, self.n, self.k)
+        self.ws = t.empty(max(self.wsb, 1), dtype=t.uint8, device="cuda")
+
+    def run(self):
+        self.xss.gpu_qselect(self.kdt, self.x.data_ptr(), self.k, self.n, False, False,
+                             self.ws.data_ptr(), self.wsb, self.stream.cuda_stream)
+
+    def _order_key(self, a):
+        t = self.torch
+        if self.kdt == "uint16":
+            return a.to(t.int32) & 0xFFFF
+        return a.view(t.float16).to(t.float32)
+
+    def check(self):
+        t = self.torch
+        kx, ky = self._order_key(self.k0), self._order_key(self.x)
+        kth = t.kthvalue(kx, self.k + 1).values
+        ok = float(ky[self.k]) == float(kth)
+        ok &= bool((ky[:self.k] <= ky[self.k]).all()) and bool((ky[self.k + 1:] >= ky[self.k]).all())
+        ok &= bool(t.equal(t.sort(ky).values, t.sort(kx).values))
+        return ok
+
+    def host_setup(self):
+        hd = np.uint16 if self.kdt == "uint16" else np.float16
+        self.hk0 = self.k0.cpu().numpy().view(hd)
+        self.hk = self.pinned(self.n * 2, hd)
+
+    def host_bytes(self):
+        return self.n * 2, self.n * 2
+
+    def cpu_sample(self, m):
+        rng = np.random.default_rng(2)
+        table = zipf16_codes(rng, self.kdt)
+        return (table[rng.choice(4096, m, p=ZIPF_P)],)
+
+    def cpu_run(self, lib, kind, sample, threads):
+        x = sample[0].copy()
+        kk = max(1, self.k * x.size // self.n)
+        assert lib.qselect(self.kid, x.ctypes.data, kk, x.size, 0, 0) == 0
+
+
+class SelectZipfF16(SelectZipf16):
+    name = "qselect_f16_zipf"
+    kdt, kid = "float16", 2
+
+
+class KeyValueSelectWorkload(SelectWorkload):
+    """keyvalue_select of 2^27 float32 keys ~ N(0,1) (seed 2) carrying uint32
+    values = original index, at k."""
+
+    name = "kv_select_f32"
+    op = "keyvalue_select"
+    kdt, kid, vdt, kb, vb = "float32", 5, "uint32", 4, 4
+    default_k = 1 << 26
+
+    def describe(self):
+        dist = "N(0,1)" if self.kdt == "float32" else "uniform full range"
+        return {"workload": f"{self.op} {self.kdt}->{self.vdt} n=2^{self.n.bit_length() - 1} "
+                            f"{dist}, values=index, k={self.k}",
+                "n": self.n, "k": self.k, "l2": "inputs larger than L2; restored per step"}
+
+    def make_keys(self, g):
+        return self.torch.randn(self.n, device="cuda", generator=g)
+
+    def setup(self):
+        t = self.torch
+        g = t.Generator(device="cuda").manual_seed(2)
+        self.k0 = self.make_keys(g)
+        self.v0 = t.arange(self.n, dtype=t.int32, device="cuda")
+        self.x = t.empty_like(self.k0)
+        self.v = t.empty_like(self.v0)
+        self.wsb = self.xss.workspace_size(self.op, self.kdt, self.n, self.k, val_dtype=self.vdt)
+        self.ws = t.empty(max(self.wsb, 1), dtype=t.uint8, device="cuda")
+
+    def restore(self):
+        self.x.copy_(self.k0)
+        self.v.copy_(self.v0)
+
+    def run(self):
+        f = (self.xss.gpu_keyvalue_partial_sort if self.op == "keyvalue_partial_sort"
+             else self.xss.gpu_keyvalue_select)
+        f(self.kdt, self.vdt, self.x.data_ptr(), self.v.data_ptr(), self.k, self.n, False, False,
+          self.ws.data_ptr(), self.wsb, self.stream.cuda_stream)
+
+    def check(self):
+        t = self.torch
+        vi = self.v.to(t.int64)
+        ok = bool(t.equal(self.k0[vi], self.x))
+        cnt = t.zeros(self.n, dtype=t.int32, device="cuda")
+        cnt.index_add_(0, vi, t.ones(self.n, dtype=t.int32, device="cuda"))
+        ok &= bool((cnt == 1).all())
+        kk = self.k - 1 if self.op == "keyvalue_partial_sort" else self.k
+        kth = t.kthvalue(self.k0, kk + 1).values
+        ok &= float(self.x[kk]) == float(kth)
+        ok &= bool((self.x[:kk] <= self.x[kk]).all()) and bool((self.x[kk + 1:] >= self.x[kk]).all())
+        if self.op == "keyvalue_partial_sort":
+            ok &= bool(t.equal(self.x[:self.k], t.sort(self.k0).values[:self.k]))
+        return ok
+
+    def bytes_model(self):    # histogram + one partition of the pairs R+W (+ sort of the top k)
+        m = self.n * self.kb + 2 * self.n * (self.kb + self.vb)
+        if self.op == "keyvalue_partial_sort":
+            m += self.k * (self.kb + 2 * self.kb * (self.kb + self.vb))
+        return m
+
+    def host_setup(self):
+        self.hk0 = self.k0.cpu().numpy()
+        self.hv0 = self.v0.cpu().numpy().view(np.uint32)
+        self.hk = self.pinned(self.n * self.kb, self.hk0.dtype)
+        self.hv = self.pinned(self.n * self.vb, np.uint32)
+
+    def host_restore(self):
+        np.copyto(self.hk, self.hk0)
+        np.copyto(self.hv, self.hv0)
+
+    def host_run(self):
+        f = (self.xss.keyvalue_partial_sort if self.op == "keyvalue_partial_sort"
+             else self.xss.keyvalue_select)
+        f(self.hk, self.hv, self.k)
+
+    def host_bytes(self):
+        return self.n * (self.kb + self.vb), self.n * (self.kb + self.vb)
+
+    def cpu_sample(self, m):
+        rng = np.random.default_rng(2)
+        if self.kdt == "float32":
+            k = rng.standard_normal(m).astype(np.float32)
+        else:
+            k = rng.integers(-2**31, 2**31 - 1, m, dtype=np.int32)
+        return (k, np.arange(m, dtype=np.uint32))
+
+    def cpu_run(self, lib, kind, sample, threads):
+        k, v = sample[0].copy(), sample[1].copy()
+        if self.op == "keyvalue_partial_sort":
+            rc = lib.keyvalue_partial_sort(self.kid, 3, k.ctypes.data, v.ctypes.data, self.k,
+                                           k.size, 0, 0)
+        else:
+            kk = max(1, self.k * k.size // self.n)
+            rc = lib.keyvalue_select(self.kid, 3, k.ctypes.data, v.ctypes.data, kk, k.size, 0, 0)
+        assert rc == 0
+
+
+class KeyValuePartialI32(KeyValueSelectWorkload):
+    """keyvalue_partial_sort of 2^27 int32 keys (uniform full range, seed 2)
+    carrying uint32 values = original index, k = 4096."""
+
+    name = "kv_partial_i32"
+    op = "keyvalue_partial_sort"
+    kdt, kid = "int32", 4
+    default_k = 4096
+
+    def make_keys(self, g):
+        t = self.torch
+        return t.randint(-2**31, 2**31 - 1, (self.n,), dtype=t.int32, device="cuda", generator=g)
+
+
+class ArgselectF32(SelectWorkload):
+    """argselect of 2^27 float32 keys ~ N(0,1) (seed 2) at k: 64-bit indices,
+    the input left as it is."""
+
+    name = "argselect_f32"
+    default_k = 1 << 26
+
+    def describe(self):
+        return {"workload": f"argselect float32 n=2^{self.n.bit_length() - 1} N(0,1) k={self.k}",
+                "n": self.n, "k": self.k, "l2": "inputs larger than L2"}
+
+    def setup(self):
+        t = self.torch
+        g = t.Generator(device="cuda").manual_seed(2)
+        self.k0 = t.randn(self.n, device="cuda", generator=g)
+        self.arg = t.empty(self.n, dtype=t.int64, device="cuda")
+        self.wsb = self.xss.workspace_size("argselect", "float32", self.n, self.k)
+        self.ws = t.empty(max(self.wsb, 1), dtype=t.uint8, device="cuda")
+
+    def restore(self):
+        self.arg.fill_(-1)
+
+    def run(self):
+        self.xss.gpu_argselect("float32", self.k0.data_ptr(), self.arg.data_ptr(), self.k,
+                               self.n, False, self.ws.data_ptr(), self.wsb,
+                               self.stream.cuda_stream)
+
+    def check(self):
+        t = self.torch
+        a = self.arg
+        ok = bool(((a >= 0) & (a < self.n)).all())
+        if not ok:
+            return False
+        cnt = t.zeros(self.n, dtype=t.int32, device="cuda")
+        cnt.index_add_(0, a, t.ones(self.n, dtype=t.int32, device="cuda"))
+        ok &= bool((cnt == 1).all())
+        x = self.k0[a]
+        kth = t.kthvalue(self.k0, self.k + 1).values
+        ok &= float(x[self.k]) == float(kth)
+        ok &= bool((x[:self.k] <= kth).all()) and bool((x[self.k + 1:] >= kth).all())
+        return ok
+
+    def bytes_model(self):    # histogram + one partition of (key, 64-bit index) R+W
+        return self.n * 4 + 2 * self.n * (4 + 8)
+
+    def host_setup(self):
+        self.hk = self.pinned(self.n * 4, np.float32)
+        np.copyto(self.hk, self.k0.cpu().numpy())
+
+    def host_restore(self):
+        pass
+
+    def host_run(self):
+        self.xss.argselect(self.hk, self.k)
+
+    def host_bytes(self):
+        return self.n * 4, self.n * 8
+
+    def cpu_run(self, lib, kind, sample, threads):
+        x = sample[0]
+        arg = np.empty(x.size, np.uint64)
+        kk = max(1, self.k * x.size // self.n)
+        assert lib.argselect(5, x.ctypes.data, arg.ctypes.data, kk, x.size, 0) == 0
+
+
+class ObjectRecords(Workload):
+    """Device object sort: 2^26 records of 24 bytes {int32 x, int32 y, float32
+    distance, 4 pad bytes, uint64 metric}, y = original position, ordered by the
+    float32 member `distance` ~ N(0,1) (seed 5) through xss_gpu_object_qsort."""
+
+    name = "object_records"
+    kb, rec, key_off = 4, 24, 8
+    dominant = None
+
+    def describe(self):
+        return {"workload": f"object_qsort of n=2^{self.n.bit_length() - 1} device records of 24 B "
+                            "{int32 x, int32 y, float32 distance, uint64 metric} by distance "
+                            "~ N(0,1)", "n": self.n,
+                "l2": "inputs larger than L2; restored per step"}
+
+    def setup(self):
+        t, n = self.torch, self.n
+        g = t.Generator(device="cuda").manual_seed(5)
+        w = t.zeros((n, 6), dtype=t.int32, device="cuda")
+        w[:, 0] = t.randint(-1000, 1000, (n,), dtype=t.int32, device="cuda", generator=g)
+        w[:, 1] = t.arange(n, dtype=t.int32, device="cuda")
+        w[:, 2] = t.randn(n, device="cuda", generator=g).view(t.int32)
+        w[:, 4:6] = t.randint(0, 2**31 - 1, (n, 2), dtype=t.int32, device="cuda", generator=g)
+        self.r0 = w.view(-1)
+        self.r = t.empty_like(self.r0)
+        self.wsb = self.xss.object_workspace_size(n, self.rec, "float32")
+        self.ws = t.empty(max(self.wsb, 1), dtype=t.uint8, device="cuda")
+
+    def restore(self):
+        self.r.copy_(self.r0)
+
+    def run(self):
+        self.xss.gpu_object_qsort(self.r.data_ptr(), self.n, self.rec, self.key_off, "float32",
+                                  False, False, self.ws.data_ptr(), self.wsb,
+                                  self.stream.cuda_stream)
+
+    def check(self):
+        t = self.torch
+        w0, w = self.r0.view(self.n, 6), self.r.view(self.n, 6)
+        d = w[:, 2].contiguous().view(t.float32)
+        ok = bool((d[1:] >= d[:-1]).all())
+        src = w[:, 1].to(t.int64)
+        ok &= bool(((src >= 0) & (src < self.n)).all())
+        if not ok:
+            return False
+        cnt = t.zeros(self.n, dtype=t.int32, device="cuda")
+        cnt.index_add_(0, src, t.ones(self.n, dtype=t.int32, device="cuda"))
+        ok &= bool((cnt == 1).all())
+        ok &= bool(t.equal(w0[src], w))
+        return ok
+
+    def passes(self):
+        return 4
+
+    def bytes_per_pass(self):
+        return 2 * self.n * (self.kb + 4)
+
+    def bytes_model(self):
+        # key read (every sector of the records holds a key) + (key, position)
+        # written, their key-value sort, the record gather R+W and the copy back
+        n, r = self.n, self.rec
+        return n * r + n * (self.kb + 4) + n * (self.kb + 2 * 4 * (self.kb + 4)) + 4 * n * r
+
+    def cpu_sample(self, m):
+        rng = np.random.default_rng(5)
+        w = np.zeros((m, 6), np.int32)
+        w[:, 0] = rng.integers(-1000, 1000, m)
+        w[:, 1] = np.arange(m)
+        w[:, 2] = rng.standard_normal(m).astype(np.float32).view(np.int32)
+        return (w,)
+
+    def cpu_run(self, lib, kind, sample, threads):
+        """The reference's object_qsort: keys read out of the objects, a key-value
+        sort of (key, position), then the objects permuted."""
+        w = sample[0].copy()
+        keys = w[:, 2].copy().view(np.float32)
+        pos = np.arange(w.shape[0], dtype=np.uint32)
+        if kind == "reference":
+            rc = lib.keyvalue_qsort(5, 3, keys.ctypes.data, pos.ctypes.data, keys.size, 0, 0)
+        else:
+            rc = lib.keyvalue_qsort_mt(5, 3, keys.ctypes.data, pos.ctypes.data, keys.size, 0, 0,
+                                       threads)
+        assert rc == 0
+        w[:] = w[pos]
+
+
+class SegmentedF32(SegmentedSort):
+    """The float32 variant of the segmented batch: keys ~ N(0,1)."""
+
+    name = "segmented_f32"
+    kdt, kid = "float32", 5
+
 SEG_LITERAL = -1
 DTYPE_OF = {"keyvalue_qsort": "int64", "qsort_f32": "f32", "segmented": "int32",
             "qsort_f32_2e20": "f32", "argsort_i64": "int64", "argsort_f64": "f64",
-            "qselect_f32": "f32", "partial_f32": "f32"}
+            "qselect_f32": "f32", "partial_f32": "f32", "segmented_f32": "f32",
+            "qselect_u16_zipf": "u16", "qselect_f16_zipf": "f16", "kv_select_f32": "f32",
+            "kv_partial_i32": "int32", "argselect_f32": "f32", "object_records": "f32"}
 WORKLOADS = {"keyvalue_qsort": (KeyValueSort, 1 << 28), "qsort_f32": (QsortF32, 1 << 28),
              "segmented": (SegmentedSort, SEG_LITERAL),
              "qsort_f32_2e20": (QsortF32Small, 1 << 20),
              "argsort_i64": (ArgsortWorkload, 1 << 28), "argsort_f64": (ArgsortF64, 1 << 28),
-             "qselect_f32": (SelectWorkload, 1 << 27), "partial_f32": (PartialWorkload, 1 << 27)}
+             "qselect_f32": (SelectWorkload, 1 << 27), "partial_f32": (PartialWorkload, 1 << 27),
+             "segmented_f32": (SegmentedF32, SEG_LITERAL),
+             "qselect_u16_zipf": (SelectZipf16, 1 << 28),
+             "qselect_f16_zipf": (SelectZipfF16, 1 << 28),
+             "kv_select_f32": (KeyValueSelectWorkload, 1 << 27),
+             "kv_partial_i32": (KeyValuePartialI32, 1 << 27),
+             "argselect_f32": (ArgselectF32, 1 << 27),
+             "object_records": (ObjectRecords, 1 << 26)}
 
 
 # ---------------------------------------------------------------------------
@@ -629,8 +1002,8 @@ def reference_arm(args):
     import torch  # noqa: F401  (only for the workload class' sample helpers)
     cls, n_full = WORKLOADS[args.workload]
     wl = cls(None, None, n_full, None)
-    if hasattr(wl, "partial"):
-        wl.k = args.k
+    if hasattr(wl, "default_k"):
+        wl.k = args.k if args.k is not None else wl.default_k
     from oracle import pyoracle
     lib, kind = pyoracle.reference(), "reference"
     if lib is None:
@@ -828,7 +1201,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--workload", default="keyvalue_qsort",
                     choices=sorted(WORKLOADS) + ["serving"])
-    ap.add_argument("--k", type=int, default=1 << 26, help="select workloads: k")
+    ap.add_argument("--k", type=int, default=None,
+                    help="select workloads: k (default: the workload's own)")
     ap.add_argument("--rate", type=float, default=20000.0, help="serving: offered req/s")
     ap.add_argument("--duration", type=float, default=2.0, help="serving: seconds of arrivals")
     ap.add_argument("--ring-gb", type=int, default=16, help="serving: pinned output ring")
@@ -840,6 +1214,8 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=1 << 24)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-percall", action="store_true",
+                    help="segmented: skip the per-segment-call comparison")
     args = ap.parse_args()
     assert args.warmup >= 3 or args.impl == "reference", "at least 3 warm-up steps"
 
@@ -867,8 +1243,8 @@ def main():
     stream = torch.cuda.Stream()
     wl = cls(torch, xss, n, stream)
     n = wl.n
-    if hasattr(wl, "partial"):
-        wl.k = args.k
+    if hasattr(wl, "default_k"):
+        wl.k = args.k if args.k is not None else wl.default_k
     flush = None
     if getattr(wl, "flush_l2", False):
         flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
@@ -941,7 +1317,7 @@ def main():
     xss.stream_status(stream.cuda_stream)
     checked = wl.check()
     percall = None
-    if hasattr(wl, "run_percall"):
+    if hasattr(wl, "run_percall") and not args.no_percall:
         # the same batch by one single-array call per segment (untimed warm-up first)
         pc = []
         for _ in range(2):

@@ -285,6 +285,10 @@ def gpu_object_qsort(d_recs, n, rec_bytes, key_offset, key_dtype, hasnan=False,
                                      stream or None), "gpu_object_qsort")
 
 
+def object_workspace_size(n, rec_bytes, key_dtype) -> int:
+    return lib().xss_gpu_object_workspace_size(n, rec_bytes, dtype_id(key_dtype))
+
+
 class SegPlan:
     """A reusable segmented-sort plan (xss_seg_plan_*) for one offsets layout."""
 
