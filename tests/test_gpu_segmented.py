@@ -100,3 +100,38 @@ def test_percall_baseline_agrees(xss, cuda):
     xss.stream_status()
     _check(k, v, dk.cpu().numpy().view(np.int32), dv.cpu().numpy().view(np.uint32), off, False,
            "per-call")
+
+
+@pytest.mark.parametrize("shape", ["constant", "smallrange", "sorted", "reverse", "random_5d"])
+@pytest.mark.parametrize("kdt,vdt", [("int32", "uint32"), ("uint64", None), ("float16", "uint64")])
+def test_segmented_mid_sizes_shapes(xss, cuda, shape, kdt, vdt):
+    """Segments of 257..4096 keys (one CTA each, radix sort in shared memory)
+    with inputs whose digits repeat: passes whose digit every key shares are
+    skipped, the others must keep the order stable."""
+    torch = cuda
+    rng = np.random.default_rng(31)
+    sizes = np.concatenate([[257, 300, 511, 512, 513, 1024, 2047, 4095, 4096],
+                            rng.integers(257, 4097, 40)]).astype(np.uint64)
+    off = np.zeros(sizes.size + 1, np.uint64)
+    off[1:] = np.cumsum(sizes)
+    n = int(off[-1])
+    k = np.concatenate([get_array(shape, kdt, int(s), 7 + i) for i, s in enumerate(sizes)])
+    v = kv_values(vdt, n, 4) if vdt else None
+    hasnan = np.dtype(kdt).kind == "f"
+    for desc in (False, True):
+        dk, dv = _dev(torch, k), (_dev(torch, v) if vdt else None)
+        doff = torch.from_numpy(off.view(np.int64).copy()).cuda()
+        xss.gpu_segmented_sort(kdt, vdt, dk.data_ptr(), dv.data_ptr() if vdt else 0,
+                               doff.data_ptr(), off, off.size - 1, hasnan, desc)
+        xss.stream_status()
+        ko = dk.cpu().numpy().view(k.dtype)
+        vo = dv.cpu().numpy().view(v.dtype) if vdt else None
+        _check(k, v, ko, vo, off, desc, f"{shape} {kdt}/{vdt} desc={desc}")
+        if vdt:
+            # stable: values of equal keys keep their input order
+            for i in range(sizes.size):
+                b, e = int(off[i]), int(off[i + 1])
+                kk = k[b:e]
+                order = np.argsort(-kk.astype(np.float64) if desc else kk, kind="stable")
+                if np.dtype(kdt).kind != "f":
+                    assert np.array_equal(vo[b:e], v[b:e][order]), f"{shape} seg {i} stability"

@@ -36,6 +36,7 @@ struct PassDesc {
     int gen_idx;     // values are the element index (argsort, first pass)
     int skip_keys;   // keys are not stored (argsort, last pass)
     int out_idx;     // values go to the 64-bit index output (argsort, last pass)
+    int tie_free;    // keys only, first pass: ties need no order (unstable ranking)
 };
 
 enum FixupMode : int { FIX_NONE = 0, FIX_COPY = 1, FIX_CANON = 2, FIX_IOTA = 3 };

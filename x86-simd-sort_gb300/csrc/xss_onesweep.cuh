@@ -250,9 +250,27 @@ __device__ __forceinline__ void pass_tile(const RadixArgs &a, const PassDesc &pd
     uint32_t *const hist32 = ps.wm;
     uint32_t *wh = hist32 + warp * RADIX;
 
-    // ---- per-warp digit counts (independent shared atomics)
+    // Keys-only first pass (pd.tie_free): equal codes are the same key and no
+    // earlier pass has ordered the tile, so ties need no order.  The tile then
+    // counts into one set of counters and each key claims its staging slot
+    // with one shared atomic, instead of the per-warp counts and lane masks
+    // that keep ties stable.
+    // Keys past the end of a partial tile (padding) are left out there: they
+    // would take slots among the real keys of the top digit.
+    const bool tie_free = !HAS_V && pd.tie_free;
+    const uint32_t valid = min((uint32_t)TILE, n - tile_base);
+    const uint32_t local0 = (uint32_t)warp * (ITEMS * 32) + lane;
+
+    // ---- digit counts (independent shared atomics): per warp, or per tile
+    if (tie_free) {
 #pragma unroll
-    for (int j = 0; j < ITEMS; ++j) atomicAdd(&wh[uint32_t(key[j] >> shift) & (RADIX - 1)], 1u);
+        for (int j = 0; j < ITEMS; ++j)
+            if (local0 + j * 32 < valid)
+                atomicAdd(&hist32[uint32_t(key[j] >> shift) & (RADIX - 1)], 1u);
+    } else {
+#pragma unroll
+        for (int j = 0; j < ITEMS; ++j) atomicAdd(&wh[uint32_t(key[j] >> shift) & (RADIX - 1)], 1u);
+    }
     __syncthreads();
 
     // ---- tile counts published at once, so successors' look-backs can pass
@@ -260,19 +278,27 @@ __device__ __forceinline__ void pass_tile(const RadixArgs &a, const PassDesc &pd
     uint32_t *st_tile = job.st_pass + (size_t)tile * RADIX;
     uint32_t cnt = 0;
     if (tid < RADIX) {
+        if (tie_free) {
+            cnt = hist32[tid];
+        } else {
 #pragma unroll
-        for (int w = 0; w < WARPS; ++w) cnt += hist32[w * RADIX + tid];
+            for (int w = 0; w < WARPS; ++w) cnt += hist32[w * RADIX + tid];
+        }
         st_relaxed_u32(st_tile + tid, (tile == job.first ? FLAG_PRE : FLAG_AGG) | cnt);
     }
     uint32_t total;
     const uint32_t local_start = block_excl_scan<BLOCK>(cnt, ps.scan, total);
     if (tid < RADIX) {
-        uint32_t run = local_start;
+        if (tie_free) {
+            hist32[tid] = local_start;
+        } else {
+            uint32_t run = local_start;
 #pragma unroll
-        for (int w = 0; w < WARPS; ++w) {
-            const uint32_t c = hist32[w * RADIX + tid];
-            hist32[w * RADIX + tid] = run;
-            run += c;
+            for (int w = 0; w < WARPS; ++w) {
+                const uint32_t c = hist32[w * RADIX + tid];
+                hist32[w * RADIX + tid] = run;
+                run += c;
+            }
         }
         ps.cnt[tid] = cnt;
         ps.lstart[tid] = local_start;
@@ -310,7 +336,12 @@ __device__ __forceinline__ void pass_tile(const RadixArgs &a, const PassDesc &pd
     // reads back (RANK 0: fewer instructions, the leader clears the word).
     // (The warp match instruction measured 1.8x slower than either.)
     // The highest such lane advances the warp's running offset for the digit.
-    {
+    if (tie_free) {
+#pragma unroll
+        for (int j = 0; j < ITEMS; ++j)
+            if (local0 + j * 32 < valid)
+                s_k[atomicAdd(&hist32[uint32_t(key[j] >> shift) & (RADIX - 1)], 1u)] = key[j];
+    } else {
         const uint32_t lt_mask = (1u << lane) - 1u;
         uint32_t *mt = hist32 + (WARPS + warp) * RADIX;   // RANK 0 only
 #pragma unroll
@@ -355,7 +386,6 @@ __device__ __forceinline__ void pass_tile(const RadixArgs &a, const PassDesc &pd
     __syncthreads();
 
     // ---- scatter runs of equal digits to consecutive global addresses
-    const uint32_t valid = min((uint32_t)TILE, n - tile_base);
 #pragma unroll
     for (int m = 0; m < ITEMS; ++m) {
         const uint32_t i = tid + m * BLOCK;
@@ -374,7 +404,8 @@ __device__ __forceinline__ void pass_tile(const RadixArgs &a, const PassDesc &pd
             }
         }
     }
-    for (int i = tid; i < PassSmem<BLOCK, RANK>::WORDS; i += BLOCK) ps.wm[i] = 0;
+    const int dirty = tie_free ? RADIX : PassSmem<BLOCK, RANK>::WORDS;
+    for (int i = tid; i < dirty; i += BLOCK) ps.wm[i] = 0;
 }
 
 struct NoAfterRank {

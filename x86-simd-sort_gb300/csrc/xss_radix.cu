@@ -121,6 +121,9 @@ __global__ void __launch_bounds__(256) hist_kernel(RadixArgs a)
             d.last = (seen == m - 1);
             d.src = cur;
             d.vsrc = cur;
+            // a keys-only sort's first pass may order ties arbitrarily: equal
+            // codes are the same key and nothing is ordered yet
+            d.tie_free = a.op == SOP_KEYS && d.first;
             if (a.op == SOP_ARG) {
                 d.dst = (cur == 1) ? 2 : 1;
                 d.vdst = d.dst;

@@ -4,8 +4,10 @@
 // once per array.  Here all segments of a batch are sorted by a fixed handful
 // of launches, whatever their number:
 //   * segments of <= 32 keys: one warp each, bitonic network in registers;
-//   * <= 256 and <= 4096 keys: one CTA each, bitonic network in shared memory
+//   * <= 256 keys: one CTA each, bitonic network in shared memory
 //     (xss_blocksort.cuh);
+//   * <= 4096 keys: one CTA each, stable LSD radix sort in shared memory
+//     (xss_blockradix.cuh);
 //   * larger segments: one segmented LSD radix sort -- the onesweep pass of
 //     xss_onesweep.cuh over the tiles of every large segment at once, with
 //     per-segment bucket starts and a look-back that stops at the first tile
@@ -18,6 +20,7 @@
 #include <mutex>
 #include <new>
 #include <vector>
+#include "xss_blockradix.cuh"
 #include "xss_blocksort.cuh"
 #include "xss_onesweep.cuh"
 
@@ -28,7 +31,8 @@ constexpr uint32_t SEG_WARP_MAX = 32;
 constexpr uint32_t SEG_SMALL_MAX = 256;
 constexpr uint32_t SEG_MED_MAX = (uint32_t)SMALL_SORT_MAX;  // 4096
 constexpr int SEG_SMALL_BLOCK = 128;
-constexpr int SEG_MED_BLOCK = 1024;
+constexpr int SEG_MED_BLOCK = 256;
+constexpr int SEG_MED_ITEMS = (int)SEG_MED_MAX / SEG_MED_BLOCK;
 
 struct SegArgs {
     void *keys;
@@ -106,6 +110,21 @@ __global__ void __launch_bounds__(BLOCK) seg_block_kernel(SegArgs a)
     if constexpr (!std::is_same<V, NoVal>::value) vals = static_cast<V *>(a.vals) + off;
     block_bitonic_sort<C, V, BLOCK, MAXN>(keys, keys, vals, vals, nullptr, len, npad, a.xf,
                                           s_raw);
+}
+
+// ---- <= 4096 keys: one CTA per segment, radix sort in shared memory --------
+template <typename C, typename V>
+__global__ void __launch_bounds__(SEG_MED_BLOCK) seg_radix_kernel(SegArgs a)
+{
+    extern __shared__ __align__(16) unsigned char s_raw[];
+    const uint32_t s = a.list[blockIdx.x];
+    const uint64_t off = a.offsets[s];
+    const uint32_t len = (uint32_t)(a.offsets[s + 1] - off);
+    C *keys = static_cast<C *>(a.keys) + off;
+    V *vals = nullptr;
+    if constexpr (!std::is_same<V, NoVal>::value) vals = static_cast<V *>(a.vals) + off;
+    block_radix_sort<C, V, SEG_MED_BLOCK, SEG_MED_ITEMS>(keys, vals, len, (int)sizeof(C), a.xf,
+                                                         s_raw);
 }
 
 // ---- large segments: histogram of every pass per segment ---------------------
@@ -407,10 +426,13 @@ static int seg_launch(const SegPlan &p, SegArgs a, cudaStream_t s)
         SegArgs b = a;
         b.list = reinterpret_cast<const uint32_t *>(ws + p.lay.med);
         b.count = (uint32_t)p.med.size();
-        const size_t smem = align_up(sizeof(C) * SEG_MED_MAX, 16) + 2 * SEG_MED_MAX;
-        XSS_LAUNCH(PK_SEG_BLOCK, ss,
-                   (seg_block_kernel<C, V, SEG_MED_BLOCK, SEG_MED_MAX>
-                    <<<b.count, SEG_MED_BLOCK, smem, ss>>>(b)));
+        const size_t smem = block_radix_smem<C, V, SEG_MED_BLOCK, SEG_MED_ITEMS>();
+        auto kern = seg_radix_kernel<C, V>;
+        {
+            const int rc = set_max_dyn_smem((const void *)kern, smem);
+            if (rc) return rc;
+        }
+        XSS_LAUNCH(PK_SEG_BLOCK, ss, (kern<<<b.count, SEG_MED_BLOCK, smem, ss>>>(b)));
         XSS_CUDA_TRY(cudaGetLastError());
     }
     if (any_large) {
