@@ -110,7 +110,7 @@ def test_segmented_mid_sizes_shapes(xss, cuda, shape, kdt, vdt):
     skipped, the others must keep the order stable."""
     torch = cuda
     rng = np.random.default_rng(31)
-    sizes = np.concatenate([[257, 300, 511, 512, 513, 1024, 2047, 4095, 4096],
+    sizes = np.concatenate([[257, 300, 511, 512, 513, 1024, 1025, 2047, 4095, 4096],
                             rng.integers(257, 4097, 40)]).astype(np.uint64)
     off = np.zeros(sizes.size + 1, np.uint64)
     off[1:] = np.cumsum(sizes)

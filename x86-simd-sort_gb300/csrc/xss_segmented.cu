@@ -33,6 +33,10 @@ constexpr uint32_t SEG_MED_MAX = (uint32_t)SMALL_SORT_MAX;  // 4096
 constexpr int SEG_SMALL_BLOCK = 128;
 constexpr int SEG_MED_BLOCK = 256;
 constexpr int SEG_MED_ITEMS = (int)SEG_MED_MAX / SEG_MED_BLOCK;
+// mid-size segments up to this many keys take a 4-keys-per-thread CTA (fewer
+// registers and less shared memory: more CTAs per SM)
+constexpr uint32_t SEG_MED1_MAX = 1024;
+constexpr int SEG_MED1_ITEMS = (int)SEG_MED1_MAX / SEG_MED_BLOCK;
 
 struct SegArgs {
     void *keys;
@@ -113,7 +117,7 @@ __global__ void __launch_bounds__(BLOCK) seg_block_kernel(SegArgs a)
 }
 
 // ---- <= 4096 keys: one CTA per segment, radix sort in shared memory --------
-template <typename C, typename V>
+template <typename C, typename V, int ITEMS>
 __global__ void __launch_bounds__(SEG_MED_BLOCK) seg_radix_kernel(SegArgs a)
 {
     extern __shared__ __align__(16) unsigned char s_raw[];
@@ -123,8 +127,7 @@ __global__ void __launch_bounds__(SEG_MED_BLOCK) seg_radix_kernel(SegArgs a)
     C *keys = static_cast<C *>(a.keys) + off;
     V *vals = nullptr;
     if constexpr (!std::is_same<V, NoVal>::value) vals = static_cast<V *>(a.vals) + off;
-    block_radix_sort<C, V, SEG_MED_BLOCK, SEG_MED_ITEMS>(keys, vals, len, (int)sizeof(C), a.xf,
-                                                         s_raw);
+    block_radix_sort<C, V, SEG_MED_BLOCK, ITEMS>(keys, vals, len, (int)sizeof(C), a.xf, s_raw);
 }
 
 // ---- large segments: histogram of every pass per segment ---------------------
@@ -275,6 +278,7 @@ struct SegPlan {
     size_t nseg, total_n;
     size_t tile;
     std::vector<uint32_t> warp, small, med, lids, ltile0, tlarge;
+    size_t med1 = 0;    // the first med1 entries of med hold <= SEG_MED1_MAX keys
     SegLayout lay;
     // graph cache for one (keys, vals, offsets, workspace) binding
     cudaGraphExec_t exec = nullptr;
@@ -321,6 +325,7 @@ static int plan_build(SegPlan &p, const uint64_t *off, size_t nseg)
     p.total_n = nseg ? off[nseg] : 0;
     p.tile = seg_tile_size(p.kb, p.vb);
     p.warp.clear(); p.small.clear(); p.med.clear(); p.lids.clear(); p.ltile0.clear(); p.tlarge.clear();
+    std::vector<uint32_t> med2;
     for (size_t i = 0; i < nseg; ++i) {
         if (off[i + 1] < off[i]) return XSS_EINVAL;
         const uint64_t len = off[i + 1] - off[i];
@@ -328,7 +333,8 @@ static int plan_build(SegPlan &p, const uint64_t *off, size_t nseg)
         if (len <= 1) continue;
         if (len <= SEG_WARP_MAX) p.warp.push_back((uint32_t)i);
         else if (len <= SEG_SMALL_MAX) p.small.push_back((uint32_t)i);
-        else if (len <= SEG_MED_MAX) p.med.push_back((uint32_t)i);
+        else if (len <= SEG_MED1_MAX) p.med.push_back((uint32_t)i);
+        else if (len <= SEG_MED_MAX) med2.push_back((uint32_t)i);
         else {
             p.ltile0.push_back((uint32_t)p.tlarge.size());
             const uint32_t l = (uint32_t)p.lids.size();
@@ -338,6 +344,8 @@ static int plan_build(SegPlan &p, const uint64_t *off, size_t nseg)
             p.tlarge.insert(p.tlarge.end(), tiles, l);
         }
     }
+    p.med1 = p.med.size();
+    p.med.insert(p.med.end(), med2.begin(), med2.end());
     const size_t L = p.lids.size(), T = p.tlarge.size(), P = p.kb;
     SegLayout &y = p.lay;
     size_t o = 0;
@@ -422,12 +430,25 @@ static int seg_launch(const SegPlan &p, SegArgs a, cudaStream_t s)
                     <<<b.count, SEG_SMALL_BLOCK, smem, ss>>>(b)));
         XSS_CUDA_TRY(cudaGetLastError());
     }
-    if (!p.med.empty()) {
+    if (p.med1 > 0) {
         SegArgs b = a;
         b.list = reinterpret_cast<const uint32_t *>(ws + p.lay.med);
-        b.count = (uint32_t)p.med.size();
+        b.count = (uint32_t)p.med1;
+        const size_t smem = block_radix_smem<C, V, SEG_MED_BLOCK, SEG_MED1_ITEMS>();
+        auto kern = seg_radix_kernel<C, V, SEG_MED1_ITEMS>;
+        {
+            const int rc = set_max_dyn_smem((const void *)kern, smem);
+            if (rc) return rc;
+        }
+        XSS_LAUNCH(PK_SEG_BLOCK, ss, (kern<<<b.count, SEG_MED_BLOCK, smem, ss>>>(b)));
+        XSS_CUDA_TRY(cudaGetLastError());
+    }
+    if (p.med.size() > p.med1) {
+        SegArgs b = a;
+        b.list = reinterpret_cast<const uint32_t *>(ws + p.lay.med) + p.med1;
+        b.count = (uint32_t)(p.med.size() - p.med1);
         const size_t smem = block_radix_smem<C, V, SEG_MED_BLOCK, SEG_MED_ITEMS>();
-        auto kern = seg_radix_kernel<C, V>;
+        auto kern = seg_radix_kernel<C, V, SEG_MED_ITEMS>;
         {
             const int rc = set_max_dyn_smem((const void *)kern, smem);
             if (rc) return rc;
