@@ -940,6 +940,87 @@ class ObjectRecords(Workload):
         w[:] = w[pos]
 
 
+class ObjectPoint3D(ObjectRecords):
+    """object_qsort of Point3D<double> {x, y, z} records (24 B) by the member x,
+    uniform [0, 1) doubles (seed 5): the shape of the reference's published
+    object-sort benchmark (misc/bench-simdobjsort.txt:16,23: n = 1,048,576 in
+    51.58 ms, n = 1e8 in 15.53 s on an unspecified AVX-512 processor).  Device
+    form (xss_gpu_object_qsort); e2e adds the copy of the records in and out."""
+
+    name = "object_point3d"
+    kb, rec, key_off = 8, 24, 0
+    flush_l2 = True
+    published = {1 << 20: (1 << 20) / 51.58e-3 / 1e9, 100_000_000: 1e8 / 15.53 / 1e9}
+    published_source = "misc/bench-simdobjsort.txt:16,23 (object_qsort Point3D<double> by x)"
+
+    def describe(self):
+        return {"workload": f"object_qsort of n={self.n} Point3D<double> records (24 B) by x, "
+                            "uniform [0,1)", "n": self.n,
+                "l2": "inputs restored per step; a 256 MiB buffer is written between steps "
+                      "(untimed), as 2^20 records fit in L2"}
+
+    def setup(self):
+        t, n = self.torch, self.n
+        g = t.Generator(device="cuda").manual_seed(5)
+        self.p0 = t.rand((n, 3), dtype=t.float64, device="cuda", generator=g)
+        self.r0 = self.p0.view(-1)
+        self.r = t.empty_like(self.r0)
+        self.wsb = self.xss.object_workspace_size(n, self.rec, "float64")
+        self.ws = t.empty(max(self.wsb, 1), dtype=t.uint8, device="cuda")
+
+    def run(self):
+        self.xss.gpu_object_qsort(self.r.data_ptr(), self.n, self.rec, self.key_off, "float64",
+                                  False, False, self.ws.data_ptr(), self.wsb,
+                                  self.stream.cuda_stream)
+
+    def check(self):
+        t = self.torch
+        w = self.r.view(self.n, 3)
+        order = t.sort(self.p0[:, 0], stable=True).indices
+        return bool(t.equal(self.p0[order], w))
+
+    def bytes_per_pass(self):
+        return 2 * self.n * (self.kb + 4)
+
+    def bytes_model(self):
+        n, r = self.n, self.rec
+        return n * r + n * (self.kb + 4) + n * (self.kb + 2 * 8 * (self.kb + 4)) + 4 * n * r
+
+    def host_setup(self):
+        self.hr0 = self.p0.cpu().numpy().reshape(-1)
+        self.hr = self.pinned(self.n * self.rec, np.float64)
+
+    def host_restore(self):
+        np.copyto(self.hr, self.hr0)
+
+    def host_run(self):
+        t = self.torch
+        src = t.from_numpy(self.hr)
+        with t.cuda.stream(self.stream):
+            self.r.copy_(src, non_blocking=True)
+            self.run()
+            src.copy_(self.r, non_blocking=True)
+        self.stream.synchronize()
+
+    def host_bytes(self):
+        return self.n * self.rec, self.n * self.rec
+
+    def cpu_sample(self, m):
+        return (np.random.default_rng(5).random((m, 3)),)
+
+    def cpu_run(self, lib, kind, sample, threads):
+        w = sample[0].copy()
+        keys = w[:, 0].copy()
+        pos = np.arange(w.shape[0], dtype=np.uint32)
+        if kind == "reference":
+            rc = lib.keyvalue_qsort(8, 3, keys.ctypes.data, pos.ctypes.data, keys.size, 0, 0)
+        else:
+            rc = lib.keyvalue_qsort_mt(8, 3, keys.ctypes.data, pos.ctypes.data, keys.size, 0, 0,
+                                       threads)
+        assert rc == 0
+        w[:] = w[pos]
+
+
 class SegmentedF32(SegmentedSort):
     """The float32 variant of the segmented batch: keys ~ N(0,1)."""
 
@@ -951,7 +1032,8 @@ DTYPE_OF = {"keyvalue_qsort": "int64", "qsort_f32": "f32", "segmented": "int32",
             "qsort_f32_2e20": "f32", "argsort_i64": "int64", "argsort_f64": "f64",
             "qselect_f32": "f32", "partial_f32": "f32", "segmented_f32": "f32",
             "qselect_u16_zipf": "u16", "qselect_f16_zipf": "f16", "kv_select_f32": "f32",
-            "kv_partial_i32": "int32", "argselect_f32": "f32", "object_records": "f32"}
+            "kv_partial_i32": "int32", "argselect_f32": "f32", "object_records": "f32",
+            "object_point3d": "f64"}
 WORKLOADS = {"keyvalue_qsort": (KeyValueSort, 1 << 28), "qsort_f32": (QsortF32, 1 << 28),
              "segmented": (SegmentedSort, SEG_LITERAL),
              "qsort_f32_2e20": (QsortF32Small, 1 << 20),
@@ -963,7 +1045,8 @@ WORKLOADS = {"keyvalue_qsort": (KeyValueSort, 1 << 28), "qsort_f32": (QsortF32, 
              "kv_select_f32": (KeyValueSelectWorkload, 1 << 27),
              "kv_partial_i32": (KeyValuePartialI32, 1 << 27),
              "argselect_f32": (ArgselectF32, 1 << 27),
-             "object_records": (ObjectRecords, 1 << 26)}
+             "object_records": (ObjectRecords, 1 << 26),
+             "object_point3d": (ObjectPoint3D, 1 << 20)}
 
 
 # ---------------------------------------------------------------------------
@@ -1373,11 +1456,16 @@ def main():
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cpu = cpu_baseline(wl, sample_n=args.cpu_sample)
 
+    # a published reference number for this exact workload (object_point3d only)
+    published = (getattr(wl, "published", None) or {}).get(n)
     if rank == 0:
         line = {
             "metric": "Gkeys/s", "value": value, "unit": "Gkeys/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": value / published if published else None,
+            **({"baseline_published": {"value": published, "unit": "Gkeys/s",
+                                       "source": wl.published_source}} if published else {}),
             "dtype": DTYPE_OF[args.workload],
             "data": "synthetic (seeded, generated on device)",
             "config": {**wl.describe(), "parallelism": f"replicas x{world}"},

@@ -3,7 +3,9 @@
 #pragma once
 // Look-back width re-measured afterwards (autotune.py --candidates): LB 8 beat LB 16 for
 // K32 (4.255 vs 4.331 ms), K64V64 (17.33 vs 17.49 ms) and DEFAULT (15.23 vs 15.35 ms);
-// those three lines use it.
+// those three lines use it.  K32 with the keys-only first pass ranking tie-free, uint32
+// keys at 2^28: LB 8 4.183 ms, LB 4 4.208, LB 32 4.758; look-back started early on 128
+// threads x 2 digits (DPT 2) 4.821, on 64 threads x 4 digits (DPT 4) 5.626 ms.
 
 // K16: 320,20,3,16,0,1,0 2.153 ms; 256,24,3,16,0,1,0 2.273 ms; 512,16,2,16,0,1,0 2.252 ms
 #ifndef XSS_CFG_K16
