@@ -25,59 +25,113 @@ namespace xss {
 // fused with clearing the look-back status words.  The last CTA to finish
 // turns the histograms into per-pass bucket starts and writes the pass plan:
 // a pass whose digit is the same for every key is skipped.
-// Lanes count into eight interleaved copies of the histograms: counter
-// (pass p, digit d, copy c) is word (p * RADIX + d) * 8 + c and lane l uses
-// copy l & 7.  A copy's words all lie in the four banks c, c+8, c+16, c+24,
-// which only the four lanes of that copy touch: random digits meet at most
-// 4-way bank conflicts (32 lanes over 32 banks average about 3.5), and a
-// digit every key shares (the top byte of floats, small-range integers)
-// costs a 4-way same-address conflict instead of 32-way.  The counters live
-// in dynamic shared memory (sizeof(C) * 8 KiB).
-constexpr int HIST_COPIES = 8;
+// Every lane counts into its own column of 16-bit counters: word
+// ((p * RADIX + d) / 2) * 32 + lane holds digits d and d + 1 (d even) of pass
+// p in its two halves, so the 32 lanes of a warp always touch 32 different
+// banks -- random digits and a digit every key shares (the top byte of
+// floats, small-range integers) alike cost one shared-memory wavefront per
+// warp and digit.  The HIST_BLOCK / 32 warps of a CTA share the columns, so
+// a CTA flushes its counters into the global histograms before any half
+// could pass 65535 (every HIST_FLUSH_KEYS keys per thread), and once at the
+// end.  The counters take sizeof(C) * 16 KiB of dynamic shared memory.
+constexpr int HIST_BLOCK = 512;
+// 16-byte loads per thread per step (fewer for 16-bit keys: eight keys each)
+template <typename C> constexpr int hist_vec_in_flight() { return sizeof(C) == 2 ? 4 : 8; }
+constexpr uint32_t HIST_FLUSH_KEYS = 65535u / (HIST_BLOCK / 32);
 template <typename C> constexpr size_t hist_smem_bytes()
 {
-    return sizeof(C) * RADIX * HIST_COPIES * sizeof(uint32_t);
+    return sizeof(C) * (RADIX / 2) * 32 * sizeof(uint32_t);
 }
+
 template <typename C>
-__global__ void __launch_bounds__(256) hist_kernel(RadixArgs a)
+__device__ __forceinline__ void hist_count(uint32_t *col, C c)
+{
+#pragma unroll
+    for (int p = 0; p < (int)sizeof(C); ++p) {
+        const uint32_t d = uint32_t(c >> (p * RADIX_BITS)) & (RADIX - 1);
+        atomicAdd(col + (p * (RADIX / 2) + (d >> 1)) * 32, 1u << ((d & 1u) << 4));
+    }
+}
+
+template <typename C>
+__global__ void __launch_bounds__(HIST_BLOCK) hist_kernel(RadixArgs a)
 {
     extern __shared__ __align__(16) uint32_t sh_all[];
-    __shared__ uint32_t s_scan[8];
+    __shared__ uint32_t s_scan[HIST_BLOCK / 32];
     __shared__ int s_last;
     __shared__ int s_active[MAX_PASSES];
-    const int tid = threadIdx.x;
+    const int tid = threadIdx.x, lane = tid & 31;
     const int P = a.passes;
-    constexpr int NW = (int)sizeof(C) * RADIX * HIST_COPIES;
-    for (int i = tid; i < NW; i += 256) sh_all[i] = 0;
+    constexpr int ROWS = (int)sizeof(C) * (RADIX / 2);   // 32 words each
+    for (int i = tid; i < ROWS * 32; i += HIST_BLOCK) sh_all[i] = 0;
     __syncthreads();
-    uint32_t *const sh = sh_all + (tid & (HIST_COPIES - 1));
+    uint32_t *const col = sh_all + lane;
+
+    // add every row's 32 columns (lanes read rotated columns: distinct banks)
+    // into the global histograms and clear them
+    auto flush = [&]() {
+        __syncthreads();
+        for (int r = tid; r < ROWS; r += HIST_BLOCK) {
+            uint32_t lo = 0, hi = 0;
+#pragma unroll 8
+            for (int i = 0; i < 32; ++i) {
+                uint32_t *w = sh_all + r * 32 + ((i + tid) & 31);
+                const uint32_t v = *w;
+                *w = 0;
+                lo += v & 0xFFFFu;
+                hi += v >> 16;
+            }
+            uint32_t *g = &a.hdr->hist[0][0] + 2 * r;
+            if (lo) atomicAdd(g, lo);
+            if (hi) atomicAdd(g + 1, hi);
+        }
+        __syncthreads();
+    };
 
     const C *src = static_cast<const C *>(a.kbuf[0]);
     const size_t n = a.n;
-    const size_t gtid = (size_t)blockIdx.x * 256 + tid;
-    const size_t stride = (size_t)gridDim.x * 256;
+    const size_t gtid = (size_t)blockIdx.x * HIST_BLOCK + tid;
+    const size_t stride = (size_t)gridDim.x * HIST_BLOCK;
     constexpr int VEC = 16 / sizeof(C);
+    constexpr int U = hist_vec_in_flight<C>();
     const bool aligned = (reinterpret_cast<uintptr_t>(src) & 15) == 0;
     const size_t nvec = aligned ? n / VEC : 0;
-    for (size_t v = gtid; v < nvec; v += stride) {
-        const uint4 q = reinterpret_cast<const uint4 *>(src)[v];
-        C e[VEC];
-        memcpy(e, &q, 16);
+    // the same number of steps in every thread of the grid, so the flushes
+    // (barriers) are reached by all threads of a CTA
+    const size_t vsteps = (nvec + (size_t)U * stride - 1) / ((size_t)U * stride);
+    uint32_t since = 0;   // keys per thread since the last flush (bound)
+    for (size_t st = 0; st < vsteps; ++st) {
+        uint4 q[U];
 #pragma unroll
-        for (int u = 0; u < VEC; ++u) {
-            const C c = to_code(e[u], a.xf);
+        for (int u = 0; u < U; ++u) {
+            const size_t v = st * U * stride + (size_t)u * stride + gtid;
+            q[u] = v < nvec ? reinterpret_cast<const uint4 *>(src)[v] : make_uint4(0, 0, 0, 0);
+        }
 #pragma unroll
-            for (int p = 0; p < (int)sizeof(C); ++p)
-                atomicAdd(&sh[(p * RADIX + (uint32_t(c >> (p * RADIX_BITS)) & (RADIX - 1))) *
-                              HIST_COPIES], 1u);
+        for (int u = 0; u < U; ++u) {
+            const size_t v = st * U * stride + (size_t)u * stride + gtid;
+            if (v < nvec) {
+                C e[VEC];
+                memcpy(e, &q[u], 16);
+#pragma unroll
+                for (int k = 0; k < VEC; ++k) hist_count<C>(col, to_code(e[k], a.xf));
+            }
+        }
+        since += U * VEC;
+        if (since + U * VEC > HIST_FLUSH_KEYS) {
+            flush();
+            since = 0;
         }
     }
-    for (size_t i = nvec * VEC + gtid; i < n; i += stride) {
-        const C c = to_code(src[i], a.xf);
-#pragma unroll
-        for (int p = 0; p < (int)sizeof(C); ++p)
-            atomicAdd(&sh[(p * RADIX + (uint32_t(c >> (p * RADIX_BITS)) & (RADIX - 1))) *
-                          HIST_COPIES], 1u);
+    const size_t rest = n - nvec * VEC;
+    const size_t ssteps = (rest + stride - 1) / stride;
+    for (size_t st = 0; st < ssteps; ++st) {
+        const size_t i = nvec * VEC + st * stride + gtid;
+        if (i < n) hist_count<C>(col, to_code(src[i], a.xf));
+        if (++since + 1 > HIST_FLUSH_KEYS) {
+            flush();
+            since = 0;
+        }
     }
 
     // clear the look-back words of every pass (multiple of 4 words, 16B aligned)
@@ -85,13 +139,7 @@ __global__ void __launch_bounds__(256) hist_kernel(RadixArgs a)
     uint4 *st4 = reinterpret_cast<uint4 *>(a.status);
     for (size_t i = gtid; i < nst4; i += stride) st4[i] = make_uint4(0, 0, 0, 0);
 
-    __syncthreads();
-    for (int i = tid; i < P * RADIX; i += 256) {
-        const uint4 *w = reinterpret_cast<const uint4 *>(sh_all + i * HIST_COPIES);
-        const uint4 x = w[0], y = w[1];
-        const uint32_t t = x.x + x.y + x.z + x.w + y.x + y.y + y.z + y.w;
-        if (t) atomicAdd(&a.hdr->hist[0][0] + i, t);
-    }
+    flush();
     __threadfence();
     __syncthreads();
     if (tid == 0) s_last = (atomicAdd(&a.hdr->done_ctr, 1u) == gridDim.x - 1);
@@ -100,11 +148,11 @@ __global__ void __launch_bounds__(256) hist_kernel(RadixArgs a)
     __threadfence();
 
     for (int p = 0; p < P; ++p) {
-        const uint32_t h = ld_relaxed_u32(&a.hdr->hist[p][tid]);
-        const int trivial = __syncthreads_or(h == (uint32_t)n);
+        const uint32_t h = tid < RADIX ? ld_relaxed_u32(&a.hdr->hist[p][tid]) : 0u;
+        const int trivial = __syncthreads_or(tid < RADIX && h == (uint32_t)n);
         uint32_t total;
-        const uint32_t ex = block_excl_scan<256>(h, s_scan, total);
-        a.hdr->start[p][tid] = ex;
+        const uint32_t ex = block_excl_scan<HIST_BLOCK>(h, s_scan, total);
+        if (tid < RADIX) a.hdr->start[p][tid] = ex;
         if (tid == 0) s_active[p] = !trivial;
     }
     __syncthreads();
@@ -363,14 +411,25 @@ static int onesweep_launch_cls(int op, KeyXform xf, void *keys, void *vals, uint
 
     XSS_CUDA_TRY(cudaMemsetAsync(a.hdr, 0, sizeof(RadixHeader), s));
     const int sms = num_sms();
-    const size_t want = (n + 256 * 16 - 1) / (256 * 16);
-    const int hist_grid = (int)std::max<size_t>(1, std::min<size_t>(want, (size_t)sms * 8));
     constexpr size_t HSMEM = hist_smem_bytes<C>();
     {
         const int rc = set_max_dyn_smem((const void *)hist_kernel<C>, HSMEM);
         if (rc) return rc;
     }
-    XSS_LAUNCH_OPT(o, PK_HIST, s, hist_kernel<C><<<hist_grid, 256, HSMEM, s>>>(a));
+    // resident CTAs per SM of the histogram kernel (measured once per key width)
+    static std::atomic<int> hist_per_sm{0};
+    int per_sm = hist_per_sm.load(std::memory_order_relaxed);
+    if (per_sm == 0) {
+        XSS_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, hist_kernel<C>,
+                                                                   HIST_BLOCK, HSMEM));
+        per_sm = std::max(per_sm, 1);
+        hist_per_sm.store(per_sm, std::memory_order_relaxed);
+    }
+    constexpr size_t PER_CTA = (size_t)HIST_BLOCK * hist_vec_in_flight<C>() * (16 / sizeof(C));
+    const size_t want = (n + PER_CTA - 1) / PER_CTA;
+    const int hist_grid =
+        (int)std::max<size_t>(1, std::min<size_t>(want, (size_t)sms * (size_t)per_sm));
+    XSS_LAUNCH_OPT(o, PK_HIST, s, hist_kernel<C><<<hist_grid, HIST_BLOCK, HSMEM, s>>>(a));
     XSS_CUDA_TRY(cudaGetLastError());
 
     const int form = LARGE ? pass_form(Cfg::PERSIST) : Cfg::PERSIST;
