@@ -25,7 +25,8 @@ namespace xss {
 // fused with clearing the look-back status words.  The last CTA to finish
 // turns the histograms into per-pass bucket starts and writes the pass plan:
 // a pass whose digit is the same for every key is skipped.
-// Every lane counts into its own column of 16-bit counters: word
+// 64-bit keys (eight digits per key): every lane counts into its own column of
+// 16-bit counters: word
 // ((p * RADIX + d) / 2) * 32 + lane holds digits d and d + 1 (d even) of pass
 // p in its two halves, so the 32 lanes of a warp always touch 32 different
 // banks -- random digits and a digit every key shares (the top byte of
@@ -35,12 +36,78 @@ namespace xss {
 // could pass 65535 (every HIST_FLUSH_KEYS keys per thread), and once at the
 // end.  The counters take sizeof(C) * 16 KiB of dynamic shared memory.
 constexpr int HIST_BLOCK = 512;
-// 16-byte loads per thread per step (fewer for 16-bit keys: eight keys each)
-template <typename C> constexpr int hist_vec_in_flight() { return sizeof(C) == 2 ? 4 : 8; }
+constexpr int HIST_VEC_IN_FLIGHT = 8;          // 16-byte loads per thread per step
 constexpr uint32_t HIST_FLUSH_KEYS = 65535u / (HIST_BLOCK / 32);
-template <typename C> constexpr size_t hist_smem_bytes()
+template <typename C> constexpr size_t hist_cols_smem_bytes()
 {
     return sizeof(C) * (RADIX / 2) * 32 * sizeof(uint32_t);
+}
+
+// The last CTA to finish turns the histograms into per-pass bucket starts
+// and writes the pass plan (a pass whose digit every key shares is skipped).
+template <int BLOCK>
+__device__ __forceinline__ void hist_finish(const RadixArgs &a, uint32_t *s_scan, int *s_active)
+{
+    __shared__ int s_last;
+    const int tid = threadIdx.x;
+    const int P = a.passes;
+    const size_t n = a.n;
+    __threadfence();
+    __syncthreads();
+    if (tid == 0) s_last = (atomicAdd(&a.hdr->done_ctr, 1u) == gridDim.x - 1);
+    __syncthreads();
+    if (!s_last) return;
+    __threadfence();
+
+    for (int p = 0; p < P; ++p) {
+        const uint32_t h = tid < RADIX ? ld_relaxed_u32(&a.hdr->hist[p][tid]) : 0u;
+        const int trivial = __syncthreads_or(tid < RADIX && h == (uint32_t)n);
+        uint32_t total;
+        const uint32_t ex = block_excl_scan<BLOCK>(h, s_scan, total);
+        if (tid < RADIX) a.hdr->start[p][tid] = ex;
+        if (tid == 0) s_active[p] = !trivial;
+    }
+    __syncthreads();
+    if (tid != 0) return;
+
+    int m = 0;
+    for (int p = 0; p < P; ++p) m += s_active[p];
+    int cur = 0, seen = 0;
+    for (int p = 0; p < P; ++p) {
+        PassDesc d = {};
+        if (s_active[p]) {
+            d.active = 1;
+            d.first = (seen == 0);
+            d.last = (seen == m - 1);
+            d.src = cur;
+            d.vsrc = cur;
+            // a keys-only sort's first pass may order ties arbitrarily: equal
+            // codes are the same key and nothing is ordered yet
+            d.tie_free = a.op == SOP_KEYS && d.first;
+            if (a.op == SOP_ARG) {
+                d.dst = (cur == 1) ? 2 : 1;
+                d.vdst = d.dst;
+                d.gen_idx = d.first;
+                d.skip_keys = d.last;
+                d.out_idx = d.last;
+            } else {
+                d.dst = 1 - cur;
+                d.vdst = d.dst;
+            }
+            cur = d.dst;
+            ++seen;
+        }
+        a.hdr->desc[p] = d;
+    }
+    int fix = FIX_NONE;
+    if (m == 0) {
+        if (a.op == SOP_ARG) fix = FIX_IOTA;
+        else if (a.op == SOP_KEYS && a.xf.canon && a.xf.kind == XK_FLOAT) fix = FIX_CANON;
+    } else if (a.op != SOP_ARG && cur == 1) {
+        fix = FIX_COPY;
+    }
+    a.hdr->fixup = fix;
+    a.hdr->num_active = m;
 }
 
 template <typename C>
@@ -54,11 +121,10 @@ __device__ __forceinline__ void hist_count(uint32_t *col, C c)
 }
 
 template <typename C>
-__global__ void __launch_bounds__(HIST_BLOCK) hist_kernel(RadixArgs a)
+__global__ void __launch_bounds__(HIST_BLOCK) hist_cols_kernel(RadixArgs a)
 {
     extern __shared__ __align__(16) uint32_t sh_all[];
     __shared__ uint32_t s_scan[HIST_BLOCK / 32];
-    __shared__ int s_last;
     __shared__ int s_active[MAX_PASSES];
     const int tid = threadIdx.x, lane = tid & 31;
     const int P = a.passes;
@@ -93,7 +159,7 @@ __global__ void __launch_bounds__(HIST_BLOCK) hist_kernel(RadixArgs a)
     const size_t gtid = (size_t)blockIdx.x * HIST_BLOCK + tid;
     const size_t stride = (size_t)gridDim.x * HIST_BLOCK;
     constexpr int VEC = 16 / sizeof(C);
-    constexpr int U = hist_vec_in_flight<C>();
+    constexpr int U = HIST_VEC_IN_FLIGHT;
     const bool aligned = (reinterpret_cast<uintptr_t>(src) & 15) == 0;
     const size_t nvec = aligned ? n / VEC : 0;
     // the same number of steps in every thread of the grid, so the flushes
@@ -140,62 +206,76 @@ __global__ void __launch_bounds__(HIST_BLOCK) hist_kernel(RadixArgs a)
     for (size_t i = gtid; i < nst4; i += stride) st4[i] = make_uint4(0, 0, 0, 0);
 
     flush();
-    __threadfence();
-    __syncthreads();
-    if (tid == 0) s_last = (atomicAdd(&a.hdr->done_ctr, 1u) == gridDim.x - 1);
-    __syncthreads();
-    if (!s_last) return;
-    __threadfence();
+    hist_finish<HIST_BLOCK>(a, s_scan, s_active);
+}
 
-    for (int p = 0; p < P; ++p) {
-        const uint32_t h = tid < RADIX ? ld_relaxed_u32(&a.hdr->hist[p][tid]) : 0u;
-        const int trivial = __syncthreads_or(tid < RADIX && h == (uint32_t)n);
-        uint32_t total;
-        const uint32_t ex = block_excl_scan<HIST_BLOCK>(h, s_scan, total);
-        if (tid < RADIX) a.hdr->start[p][tid] = ex;
-        if (tid == 0) s_active[p] = !trivial;
-    }
+// 16- and 32-bit keys (measured faster this way than with lane columns, which
+// hold fewer resident warps): lanes count into eight interleaved copies of the
+// histograms -- counter (pass p, digit d, copy c) is word (p * RADIX + d) * 8
+// + c and lane l uses copy l & 7.  A copy's words all lie in the four banks c,
+// c+8, c+16, c+24, which only the four lanes of that copy touch: random digits
+// meet at most 4-way bank conflicts, and a digit every key shares costs a
+// 4-way same-address conflict instead of 32-way.  sizeof(C) * 8 KiB of
+// dynamic shared memory, 256-thread CTAs.
+constexpr int HIST_COPIES = 8;
+template <typename C> constexpr size_t hist_copies_smem_bytes()
+{
+    return sizeof(C) * RADIX * HIST_COPIES * sizeof(uint32_t);
+}
+template <typename C>
+__global__ void __launch_bounds__(256) hist_copies_kernel(RadixArgs a)
+{
+    extern __shared__ __align__(16) uint32_t sh_all[];
+    __shared__ uint32_t s_scan[8];
+    __shared__ int s_active[MAX_PASSES];
+    const int tid = threadIdx.x;
+    const int P = a.passes;
+    constexpr int NW = (int)sizeof(C) * RADIX * HIST_COPIES;
+    for (int i = tid; i < NW; i += 256) sh_all[i] = 0;
     __syncthreads();
-    if (tid != 0) return;
+    uint32_t *const sh = sh_all + (tid & (HIST_COPIES - 1));
 
-    int m = 0;
-    for (int p = 0; p < P; ++p) m += s_active[p];
-    int cur = 0, seen = 0;
-    for (int p = 0; p < P; ++p) {
-        PassDesc d = {};
-        if (s_active[p]) {
-            d.active = 1;
-            d.first = (seen == 0);
-            d.last = (seen == m - 1);
-            d.src = cur;
-            d.vsrc = cur;
-            // a keys-only sort's first pass may order ties arbitrarily: equal
-            // codes are the same key and nothing is ordered yet
-            d.tie_free = a.op == SOP_KEYS && d.first;
-            if (a.op == SOP_ARG) {
-                d.dst = (cur == 1) ? 2 : 1;
-                d.vdst = d.dst;
-                d.gen_idx = d.first;
-                d.skip_keys = d.last;
-                d.out_idx = d.last;
-            } else {
-                d.dst = 1 - cur;
-                d.vdst = d.dst;
-            }
-            cur = d.dst;
-            ++seen;
+    const C *src = static_cast<const C *>(a.kbuf[0]);
+    const size_t n = a.n;
+    const size_t gtid = (size_t)blockIdx.x * 256 + tid;
+    const size_t stride = (size_t)gridDim.x * 256;
+    constexpr int VEC = 16 / sizeof(C);
+    const bool aligned = (reinterpret_cast<uintptr_t>(src) & 15) == 0;
+    const size_t nvec = aligned ? n / VEC : 0;
+    for (size_t v = gtid; v < nvec; v += stride) {
+        const uint4 q = reinterpret_cast<const uint4 *>(src)[v];
+        C e[VEC];
+        memcpy(e, &q, 16);
+#pragma unroll
+        for (int u = 0; u < VEC; ++u) {
+            const C c = to_code(e[u], a.xf);
+#pragma unroll
+            for (int p = 0; p < (int)sizeof(C); ++p)
+                atomicAdd(&sh[(p * RADIX + (uint32_t(c >> (p * RADIX_BITS)) & (RADIX - 1))) *
+                              HIST_COPIES], 1u);
         }
-        a.hdr->desc[p] = d;
     }
-    int fix = FIX_NONE;
-    if (m == 0) {
-        if (a.op == SOP_ARG) fix = FIX_IOTA;
-        else if (a.op == SOP_KEYS && a.xf.canon && a.xf.kind == XK_FLOAT) fix = FIX_CANON;
-    } else if (a.op != SOP_ARG && cur == 1) {
-        fix = FIX_COPY;
+    for (size_t i = nvec * VEC + gtid; i < n; i += stride) {
+        const C c = to_code(src[i], a.xf);
+#pragma unroll
+        for (int p = 0; p < (int)sizeof(C); ++p)
+            atomicAdd(&sh[(p * RADIX + (uint32_t(c >> (p * RADIX_BITS)) & (RADIX - 1))) *
+                          HIST_COPIES], 1u);
     }
-    a.hdr->fixup = fix;
-    a.hdr->num_active = m;
+
+    // clear the look-back words of every pass (multiple of 4 words, 16B aligned)
+    const size_t nst4 = (size_t)P * a.num_tiles * RADIX / 4;
+    uint4 *st4 = reinterpret_cast<uint4 *>(a.status);
+    for (size_t i = gtid; i < nst4; i += stride) st4[i] = make_uint4(0, 0, 0, 0);
+
+    __syncthreads();
+    for (int i = tid; i < P * RADIX; i += 256) {
+        const uint4 *w = reinterpret_cast<const uint4 *>(sh_all + i * HIST_COPIES);
+        const uint4 x = w[0], y = w[1];
+        const uint32_t t = x.x + x.y + x.z + x.w + y.x + y.y + y.z + y.w;
+        if (t) atomicAdd(&a.hdr->hist[0][0] + i, t);
+    }
+    hist_finish<256>(a, s_scan, s_active);
 }
 
 // ---------------------------------------------------------------------------
@@ -411,25 +491,37 @@ static int onesweep_launch_cls(int op, KeyXform xf, void *keys, void *vals, uint
 
     XSS_CUDA_TRY(cudaMemsetAsync(a.hdr, 0, sizeof(RadixHeader), s));
     const int sms = num_sms();
-    constexpr size_t HSMEM = hist_smem_bytes<C>();
-    {
-        const int rc = set_max_dyn_smem((const void *)hist_kernel<C>, HSMEM);
-        if (rc) return rc;
+    if constexpr (sizeof(C) == 8) {
+        constexpr size_t HSMEM = hist_cols_smem_bytes<C>();
+        {
+            const int rc = set_max_dyn_smem((const void *)hist_cols_kernel<C>, HSMEM);
+            if (rc) return rc;
+        }
+        // resident CTAs per SM of the histogram kernel (measured once)
+        static std::atomic<int> hist_per_sm{0};
+        int per_sm = hist_per_sm.load(std::memory_order_relaxed);
+        if (per_sm == 0) {
+            XSS_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                &per_sm, hist_cols_kernel<C>, HIST_BLOCK, HSMEM));
+            per_sm = std::max(per_sm, 1);
+            hist_per_sm.store(per_sm, std::memory_order_relaxed);
+        }
+        constexpr size_t PER_CTA = (size_t)HIST_BLOCK * HIST_VEC_IN_FLIGHT * (16 / sizeof(C));
+        const size_t want = (n + PER_CTA - 1) / PER_CTA;
+        const int hist_grid =
+            (int)std::max<size_t>(1, std::min<size_t>(want, (size_t)sms * (size_t)per_sm));
+        XSS_LAUNCH_OPT(o, PK_HIST, s,
+                       hist_cols_kernel<C><<<hist_grid, HIST_BLOCK, HSMEM, s>>>(a));
+    } else {
+        const size_t want = (n + 256 * 16 - 1) / (256 * 16);
+        const int hist_grid = (int)std::max<size_t>(1, std::min<size_t>(want, (size_t)sms * 8));
+        constexpr size_t HSMEM = hist_copies_smem_bytes<C>();
+        {
+            const int rc = set_max_dyn_smem((const void *)hist_copies_kernel<C>, HSMEM);
+            if (rc) return rc;
+        }
+        XSS_LAUNCH_OPT(o, PK_HIST, s, hist_copies_kernel<C><<<hist_grid, 256, HSMEM, s>>>(a));
     }
-    // resident CTAs per SM of the histogram kernel (measured once per key width)
-    static std::atomic<int> hist_per_sm{0};
-    int per_sm = hist_per_sm.load(std::memory_order_relaxed);
-    if (per_sm == 0) {
-        XSS_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, hist_kernel<C>,
-                                                                   HIST_BLOCK, HSMEM));
-        per_sm = std::max(per_sm, 1);
-        hist_per_sm.store(per_sm, std::memory_order_relaxed);
-    }
-    constexpr size_t PER_CTA = (size_t)HIST_BLOCK * hist_vec_in_flight<C>() * (16 / sizeof(C));
-    const size_t want = (n + PER_CTA - 1) / PER_CTA;
-    const int hist_grid =
-        (int)std::max<size_t>(1, std::min<size_t>(want, (size_t)sms * (size_t)per_sm));
-    XSS_LAUNCH_OPT(o, PK_HIST, s, hist_kernel<C><<<hist_grid, HIST_BLOCK, HSMEM, s>>>(a));
     XSS_CUDA_TRY(cudaGetLastError());
 
     const int form = LARGE ? pass_form(Cfg::PERSIST) : Cfg::PERSIST;
