@@ -989,17 +989,18 @@ class ObjectPoint3D(ObjectRecords):
     def host_setup(self):
         self.hr0 = self.p0.cpu().numpy().reshape(-1)
         self.hr = self.pinned(self.n * self.rec, np.float64)
+        self.hr_t = self._pinned[-1]          # the pinned tensor behind self.hr
 
     def host_restore(self):
         np.copyto(self.hr, self.hr0)
 
     def host_run(self):
         t = self.torch
-        src = t.from_numpy(self.hr)
+        dev = self.r.view(t.uint8)
         with t.cuda.stream(self.stream):
-            self.r.copy_(src, non_blocking=True)
+            dev.copy_(self.hr_t, non_blocking=True)
             self.run()
-            src.copy_(self.r, non_blocking=True)
+            self.hr_t.copy_(dev, non_blocking=True)
         self.stream.synchronize()
 
     def host_bytes(self):
