@@ -342,13 +342,8 @@ __global__ void __launch_bounds__(256) sel_split_kernel(SelArgs a, int lo, int b
             ok[q] = b0 != ~0ull;
             slot[q] = b0 + (q < 6 ? ((w[q >> 1] >> ((q & 1) * 16)) & 0xFFFFu) : w[3]);
         }
-        // a thread with nothing to record in this chunk skips the write loop
-        // (every thread still reaches the barrier below)
-        constexpr uint32_t NONE = IPT * 4 >= 32 ? 0xFFFFFFFFu : ((1u << (IPT * 4)) - 1u);
-        const bool writes = tags != NONE || candm != 0u;
 #pragma unroll
         for (int j = 0; j < IPT; ++j) {
-            if (!writes) break;
             const size_t p = p0 + j;
             const uint32_t X = (tags >> (4 * j)) & 3u, R = (tags >> (4 * j + 2)) & 3u;
 #pragma unroll
