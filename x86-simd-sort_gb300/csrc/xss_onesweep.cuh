@@ -7,8 +7,9 @@
 //                            prefetch the next tile with a bulk copy (TMA).
 // Replaces the reference's vectorised partition sweeps
 // (src/xss-common-qsort.h:252-524, src/xss-common-keyvaluesort.hpp:109-379,
-// src/xss-common-argsort.h:174-422): each pass is a stable counting scatter
-// instead of an unstable in-place partition.
+// src/xss-common-argsort.h:174-422): each pass is a counting scatter instead
+// of an unstable in-place partition, stable wherever ties can be told apart
+// (every pass but a keys-only sort's first).
 #pragma once
 #include <type_traits>
 #include "xss_internal.cuh"
