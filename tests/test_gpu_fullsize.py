@@ -153,3 +153,26 @@ def test_keyvalue_select_f32_index_2e27(xss, cuda):
     assert float(k[kk]) == float(torch.kthvalue(k0, kk + 1).values)
     assert bool((k[:kk] <= k[kk]).all()) and bool((k[kk + 1:] >= k[kk]).all())
     assert bool((k0[v.long()] == k).all())
+
+
+@pytest.mark.parametrize("shape", ["uniform", "smallrange"])
+def test_qsort_int64_2e29_histogram_flushes(xss, cuda, shape):
+    """2^29 64-bit keys: each histogram thread counts more keys than its 16-bit
+    counter columns hold at once, so the counters are flushed mid-run; with a
+    few distinct values every key of a column lands on the same counters."""
+    torch = cuda
+    n = 1 << 29
+    g = torch.Generator(device="cuda").manual_seed(6)
+    if shape == "uniform":
+        x = torch.randint(0, 256, (n * 8,), dtype=torch.uint8, device="cuda",
+                          generator=g).view(torch.int64)
+    else:
+        x = torch.randint(-3, 4, (n,), dtype=torch.int64, device="cuda", generator=g)
+    y = x.clone()
+    xss.gpu_qsort("int64", y.data_ptr(), n)
+    xss.stream_status()
+    assert bool((y[1:] >= y[:-1]).all())
+    if shape == "smallrange":
+        assert torch.equal(torch.bincount(y + 3, minlength=7), torch.bincount(x + 3, minlength=7))
+    else:
+        assert torch.equal(y, torch.sort(x).values)
