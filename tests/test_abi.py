@@ -78,3 +78,20 @@ def test_invalid_arguments_rejected_before_any_device_work(xss):
     assert L.xss_gpu_object_qsort(a.ctypes.data, 4, 16, 12, 6, 0, 0, None, 0, None) == 1  # past end
     assert L.xss_qsort(5, a.ctypes.data, 1, 0, 0) == 0            # n <= 1 is a no-op
     assert L.xss_qselect(5, a.ctypes.data, 0, 0, 0, 0) == 0       # empty select
+
+
+def test_headers_compile_and_link_without_a_gpu(xss, tmp_path):
+    """The C header is plain C, and the C++ drop-in and static headers compile
+    and link a caller program against the library (nothing is run here)."""
+    inc = os.path.join(ROOT, "include")
+    c_src = tmp_path / "abi.c"
+    c_src.write_text('#include "xss_gpu.h"\nint main(void) { return xss_strerror(0) ? 0 : 1; }\n')
+    subprocess.run(["gcc", "-std=c99", "-Wall", "-Werror", "-I", inc, "-c", str(c_src), "-o",
+                    str(tmp_path / "abi.o")], check=True)
+    cuda_home = os.environ.get("CUDA_HOME", "/usr/local/cuda")
+    pkg = os.path.dirname(xss.LIB_PATH)
+    subprocess.run(["g++", "-std=c++17", "-O0", "-I", inc, "-I", os.path.join(cuda_home, "include"),
+                    os.path.join(ROOT, "tests", "cxx", "test_api.cpp"), "-o",
+                    str(tmp_path / "test_api"), "-L", pkg, "-lxss_gb300", "-L",
+                    os.path.join(cuda_home, "lib64"), "-lcudart"], check=True)
+    assert (tmp_path / "test_api").exists()
