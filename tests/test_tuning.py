@@ -39,3 +39,11 @@ def test_committed_header_covers_every_class():
             assert macro in lines, macro
             f = [int(x) for x in lines[macro].split(",")]
             assert len(f) == 7 and f[0] % 32 == 0 and f[4] in (0, 1)
+
+
+def test_a_candidate_line_builds_into_its_own_library():
+    """The tuner's variant build (one pre-included line, the radix unit
+    recompiled, linked with the shared objects) works without a GPU."""
+    common = autotune.build_common()
+    so = autotune.build_variant("K32", "320,20,3,8,0,1,0", common)
+    assert os.path.exists(so) and os.path.getsize(so) > 0

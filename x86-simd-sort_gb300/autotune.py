@@ -80,6 +80,7 @@ def _run(cmd, **kw):
 def build_variant(cls: str, line: str, common_objs: list) -> str:
     """Compile the radix unit with one candidate line pre-included; link a library."""
     tag = f"{cls}_{line.replace(',', '_')}"
+    os.makedirs(TUNE_DIR, exist_ok=True)
     hdr = os.path.join(TUNE_DIR, f"cfg_{tag}.h")
     with open(hdr, "w") as f:
         f.write(f"#define {_base(cls)[1]} {line}\n")
