@@ -53,8 +53,8 @@ def _peaks():
 
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per launch of the
 # dominant kernel at the workload's full size: one ncu capture of a smaller case
-# scaled by the keys per launch (profiles/onesweep_kv_i64u64_2e25.md x8,
-# profiles/onesweep_f32_2e26.md: the mean of its four passes x4).
+# scaled by the keys per launch (the int64 -> uint64 pass captured at 2^25
+# keys x8; the float32 passes captured at 2^26 keys, their mean x4).
 TRAFFIC = {"keyvalue_qsort": 8245616640, "qsort_f32": 1989168640}
 
 

@@ -140,9 +140,14 @@ int xss_gpu_keyvalue_partial_sort(int key_dtype, int val_dtype, void *d_keys,
  *
  * The call is synchronous: it returns once the sort on `stream` is done, with
  * XSS_OK or XSS_ETIMEOUT from the device-side checks.  The first call on each
- * device looks up the array's device address; make that first call before any
- * stream capture.  All calls share the one array: calls whose GPU work could
- * overlap (other streams, other host threads) must be serialised by the caller.
+ * device is its set-up: it looks up the array's device address and loads onto
+ * that device every kernel a call can launch (CUDA loads kernel code lazily,
+ * and that load does allocate device memory), by sorting small arrays inside
+ * the array itself.  Make that first call once per device, outside the code
+ * that must not allocate, and before any stream capture; every later call on
+ * the device allocates nothing.  All calls share the one array and find the
+ * previous call's data in it: calls whose GPU work could overlap (other
+ * streams, other host threads) race on it and must be serialised by the caller.
  */
 #define XSS_NOALLOC_MAX_N ((size_t)1 << 20)
 int xss_gpu_qsort_noalloc(int dtype, void *d_arr, size_t n, int hasnan, int descending,

@@ -14,7 +14,8 @@ import subprocess
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_SO = os.path.join(HERE, "_build", "libxss_oracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libxss_refshim.so")
-REF_SRC = os.environ.get("XSS_REFERENCE_SRC", "/root/reference")
+# the reference's source tree, when given (build_reference argument or this variable)
+REF_SRC = os.environ.get("XSS_REFERENCE_SRC")
 
 _P, _Z, _I = ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int
 _FUNCS = {
@@ -56,11 +57,14 @@ def build_oracle() -> str:
     return ORACLE_SO
 
 
-def build_reference() -> str | None:
-    """Compile the reference from its sources into oracle/_ref when possible."""
-    if not os.path.isdir(REF_SRC) or os.uname().machine not in ("x86_64", "AMD64"):
+def build_reference(src: str | None = None) -> str | None:
+    """Compile the reference from its sources (``src``, else $XSS_REFERENCE_SRC)
+    into oracle/_ref when possible; None where no source tree is given or the
+    host cannot build it (the reference's SIMD paths need x86-64)."""
+    src = src or REF_SRC
+    if not src or not os.path.isdir(src) or os.uname().machine not in ("x86_64", "AMD64"):
         return None
-    r = subprocess.run(["make", "-s", "-j5", "-C", HERE, "ref", f"REF={REF_SRC}"])
+    r = subprocess.run(["make", "-s", "-j5", "-C", HERE, "ref", f"REF={src}"])
     return REF_SO if r.returncode == 0 and os.path.exists(REF_SO) else None
 
 

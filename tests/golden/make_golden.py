@@ -77,7 +77,9 @@ def cases():
 def main():
     ref = pyoracle.reference()
     if ref is None:
-        pyoracle.build_reference()
+        # the reference's source tree: $XSS_REFERENCE_SRC, else where this
+        # fixture generator was run against it
+        pyoracle.build_reference(os.environ.get("XSS_REFERENCE_SRC", "/root/reference"))
         ref = pyoracle.reference()
     if ref is None:
         sys.exit("reference library not buildable on this host")

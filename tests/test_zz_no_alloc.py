@@ -6,7 +6,9 @@ memory, a fixed-budget real-time loop).  Its output must equal xss_gpu_qsort's
 for the same input, call after call, although every call reuses one fixed
 scratch array.  This file is collected last so that a stop-at-first-failure
 run has already run every other test; it also passes on its own in a fresh
-process.
+process.  The first call on a device is its set-up (it loads the kernels, which
+allocates); the memory test checks that later calls leave the device's free
+memory unchanged.
 """
 import ctypes
 
@@ -66,3 +68,27 @@ def test_noalloc_rejects_sizes_above_its_limit(xss, cuda):
     rc = f(DT["float32"], a.data_ptr(), n, 0, 0, None)
     assert rc == 6  # XSS_ETOOBIG
     assert np.array_equal(a.cpu().numpy(), x)  # untouched
+
+
+def test_noalloc_leaves_device_free_memory_unchanged(xss, cuda):
+    torch = cuda
+    f = _noalloc(xss)
+    stream = torch.cuda.Stream()
+    cases = []
+    for dtype in ("uint16", "float32", "int64"):
+        for n in (3000, MAX_N):
+            x = get_array("random", dtype, n, seed=7 + n)
+            cases.append((dtype, n, torch.from_numpy(x.view(np.uint8).copy()).cuda()))
+    # set-up call (first on this device, or a repeat when earlier tests ran)
+    x0 = torch.zeros(5000, dtype=torch.float32, device="cuda")
+    assert f(DT["float32"], x0.data_ptr(), 5000, 0, 0, stream.cuda_stream) == 0
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    for _ in range(2):
+        for dtype, n, a in cases:
+            assert f(DT[dtype], a.data_ptr(), n, 1, 0, stream.cuda_stream) == 0
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    # a cudaMalloc (the library's workspace cache, a lazily loaded kernel)
+    # would take at least one 2 MiB page of device memory
+    assert free1 == free0, (free0, free1)

@@ -66,7 +66,7 @@ struct RadixArgs {
     unsigned *err;         // device-visible error word
 };
 
-inline size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+constexpr size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
 // Device-visible error word (mapped pinned host memory); see xss_capi.cu.
 unsigned *device_error_word();

@@ -549,7 +549,11 @@ __global__ void __launch_bounds__(BLOCK, MINB) onesweep_persist_kernel(RadixArgs
         C key[ITEMS];
         VS val[ITEMS];
         if (by_tma(tile)) {
-            mbar_wait_bounded(&s_bar[cur], parity[cur], a.err);
+            // a copy that never landed (the error word is already set): this
+            // CTA neither reads nor reuses that buffer and claims no further
+            // tile; its successors' look-backs give up with the same flag
+            const bool landed = mbar_wait_bounded(&s_bar[cur], parity[cur], a.err);
+            if (__syncthreads_or(!landed)) break;
             parity[cur] ^= 1u;
 #pragma unroll
             for (int j = 0; j < ITEMS; ++j) {

@@ -308,7 +308,7 @@ struct RadixLayout {
     size_t hdr, status, k1, k2, v1, v2, total;
 };
 
-static RadixLayout radix_layout(int op, int kbytes, int vbytes, size_t n, size_t tile)
+static constexpr RadixLayout radix_layout(int op, int kbytes, int vbytes, size_t n, size_t tile)
 {
     RadixLayout L{};
     const int passes = kbytes;  // 8-bit digits
@@ -333,7 +333,7 @@ static bool use_mid_lines(size_t n) { return n <= XSS_MID_N || t_prefer_shared_s
 // Tile of the lines a sort of n keys may use: for n above XSS_MID_N both
 // classes are possible (see set_prefer_shared_sm), so the workspace is sized
 // for the smaller tile, which needs the larger look-back array.
-template <typename C, typename V> static size_t tile_of(size_t n)
+template <typename C, typename V> static constexpr size_t tile_of(size_t n)
 {
     return n <= XSS_MID_N ? pass_tile_size_mid<C, V>()
                           : std::min(pass_tile_size_mid<C, V>(), pass_tile_size<C, V>());
@@ -630,12 +630,52 @@ constexpr size_t NOALLOC_ERR_BYTES = 256;                       // error word sl
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_SCRATCH_BYTES];
 
+// The scratch layout of the largest call fits the array for every key width
+// with the tuned tile sizes (a tuning line that breaks this fails the build).
+constexpr size_t NOALLOC_WS_BYTES = NOALLOC_SCRATCH_BYTES - NOALLOC_ERR_BYTES;
+static_assert(NOALLOC_MAX_N <= XSS_MID_N, "calls up to the limit use the mid-size lines");
+static_assert(radix_layout(SOP_KEYS, 2, 0, NOALLOC_MAX_N,
+                           tile_of<uint16_t, NoVal>(NOALLOC_MAX_N)).total <= NOALLOC_WS_BYTES,
+              "16-bit scratch layout exceeds the static array");
+static_assert(radix_layout(SOP_KEYS, 4, 0, NOALLOC_MAX_N,
+                           tile_of<uint32_t, NoVal>(NOALLOC_MAX_N)).total <= NOALLOC_WS_BYTES,
+              "32-bit scratch layout exceeds the static array");
+static_assert(radix_layout(SOP_KEYS, 8, 0, NOALLOC_MAX_N,
+                           tile_of<uint64_t, NoVal>(NOALLOC_MAX_N)).total <= NOALLOC_WS_BYTES,
+              "64-bit scratch layout exceeds the static array");
+
 // Device address of g_noalloc_scratch, looked up once per device.  In host
 // code the symbol itself is only a host-side stand-in, never a device address.
 static std::mutex g_noalloc_mu;
 static unsigned char *g_noalloc_addr[64];
 
-static int noalloc_scratch(unsigned char **out)
+// Per-device set-up of the first call, with that device current: look up the
+// array's device address, then load every kernel a call can launch.  CUDA
+// loads a kernel's code onto a device when it is first used (lazy loading),
+// and that load allocates device memory; so the set-up sorts, inside the
+// array itself, a small (one-CTA) and a mid-size (radix) array of each key
+// width, synchronously.  Later calls on the device allocate nothing.
+static int noalloc_prepare(unsigned char *scratch, cudaStream_t s)
+{
+    const LaunchOpts o{reinterpret_cast<unsigned *>(scratch), false};
+    XSS_CUDA_TRY(cudaMemsetAsync(scratch, 0, NOALLOC_ERR_BYTES, s));
+    for (int kbytes : {2, 4, 8}) {
+        for (size_t n : {size_t(64), SMALL_SORT_MAX + 904}) {
+            const size_t wsb = align_up(radix_workspace_bytes(SOP_KEYS, kbytes, 0, n), 256);
+            unsigned char *ws = scratch + NOALLOC_ERR_BYTES;
+            unsigned char *keys = ws + wsb;
+            if (wsb + n * kbytes > NOALLOC_WS_BYTES) return XSS_ENOMEM;
+            XSS_CUDA_TRY(cudaMemsetAsync(keys, 0, n * kbytes, s));
+            const int rc = radix_sort_opts(SOP_KEYS, kbytes, KeyXform{XK_UINT, 0, 0}, keys,
+                                           nullptr, 0, nullptr, n, ws, wsb, s, o);
+            if (rc) return rc;
+        }
+    }
+    XSS_CUDA_TRY(cudaStreamSynchronize(s));
+    return XSS_OK;
+}
+
+static int noalloc_scratch(cudaStream_t s, unsigned char **out)
 {
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return XSS_ECUDA;
@@ -647,6 +687,8 @@ static int noalloc_scratch(unsigned char **out)
             cudaGetLastError();
             return XSS_ECUDA;
         }
+        const int rc = noalloc_prepare(static_cast<unsigned char *>(p), s);
+        if (rc) return rc;
         g_noalloc_addr[dev] = static_cast<unsigned char *>(p);
     }
     *out = g_noalloc_addr[dev];
@@ -675,20 +717,15 @@ extern "C" int xss_gpu_qsort_noalloc(int dtype, void *d_arr, size_t n, int hasna
     if (n > NOALLOC_MAX_N) return XSS_ETOOBIG;
     if (n > 1 && d_arr == nullptr) return XSS_EINVAL;
     if (n <= 1) return XSS_OK;
-    // the scratch layout for the largest call must fit the array
-    if (radix_workspace_bytes(SOP_KEYS, kbytes, 0, NOALLOC_MAX_N) >
-        NOALLOC_SCRATCH_BYTES - NOALLOC_ERR_BYTES)
-        return XSS_ENOMEM;
     cudaStream_t s = (cudaStream_t)stream;
     unsigned char *scratch = nullptr;
-    int rc = noalloc_scratch(&scratch);
+    int rc = noalloc_scratch(s, &scratch);
     if (rc) return rc;
     XSS_CUDA_TRY(cudaMemsetAsync(scratch, 0, NOALLOC_ERR_BYTES, s));
     const KeyXform xf{kind, descending ? 1 : 0, hasnan ? 1 : 0};
     const LaunchOpts o{reinterpret_cast<unsigned *>(scratch), false};
     rc = radix_sort_opts(SOP_KEYS, kbytes, xf, d_arr, nullptr, 0, nullptr, n,
-                         scratch + NOALLOC_ERR_BYTES, NOALLOC_SCRATCH_BYTES - NOALLOC_ERR_BYTES,
-                         s, o);
+                         scratch + NOALLOC_ERR_BYTES, NOALLOC_WS_BYTES, s, o);
     if (rc) return rc;
     unsigned h = 0;
     XSS_CUDA_TRY(cudaMemcpyAsync(&h, scratch, sizeof(h), cudaMemcpyDeviceToHost, s));

@@ -30,7 +30,7 @@ __global__ void __launch_bounds__(32) selftest_mbar_kernel(unsigned *err, uint32
     }
     __syncthreads();
     // no arrival and no copy is ever issued: phase 0 never completes
-    mbar_wait_bounded(&bar, 0u, err, limit);
+    (void)mbar_wait_bounded(&bar, 0u, err, limit);
 }
 
 }  // namespace xss

@@ -61,18 +61,20 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity)
     return ok != 0;
 }
 
-// Bounded wait for phase `parity` of `bar`.  On expiry the error word gets
-// XSS_DEVERR_TIMEOUT and the wait continues for a second bounded period so
-// that the copy in flight normally still lands before the buffer is reused;
-// after that the caller proceeds (results are then flagged invalid).
-__device__ __forceinline__ void mbar_wait_bounded(uint64_t *bar, uint32_t parity, unsigned *err,
+// Bounded wait for phase `parity` of `bar`; true once the phase completed.
+// On expiry the error word gets XSS_DEVERR_TIMEOUT and the wait continues for
+// a second bounded period so that a copy still in flight normally lands
+// before the CTA leaves; false means it did not, and the caller must neither
+// read nor reuse the buffer (the pass kernel then stops claiming tiles).
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity, unsigned *err,
                                                   uint32_t spin_limit = XSS_SPIN_LIMIT)
 {
     uint32_t spins = 0;
     while (!mbar_try_wait(bar, parity)) {
         if (++spins == spin_limit) atomicOr(err, XSS_DEVERR_TIMEOUT);
-        if (spins >= 2 * spin_limit) break;
+        if (spins >= 2 * spin_limit) return false;
     }
+    return true;
 }
 
 }  // namespace xss
