@@ -124,6 +124,19 @@ class Workload:
         self._pinned.append(t)
         return t.numpy().view(dtype)
 
+    def release(self):
+        """Drop the workload's device and pinned buffers (several workloads run
+        one after another in the default bench)."""
+        plan = getattr(self, "plan", None)
+        if plan is not None:
+            plan.close()
+        for k in list(vars(self)):
+            v = getattr(self, k)
+            if k == "plan" or k == "_pinned" or isinstance(v, np.ndarray) or \
+                    (self.torch is not None and isinstance(v, self.torch.Tensor)):
+                if k not in ("sizes", "off"):
+                    setattr(self, k, None)
+
 
 class KeyValueSort(Workload):
     name = "keyvalue_qsort"
@@ -197,13 +210,19 @@ class KeyValueSort(Workload):
         return (rng.integers(np.iinfo(np.int64).min, np.iinfo(np.int64).max, m, dtype=np.int64),
                 np.arange(m, dtype=np.uint64))
 
-    def cpu_run(self, lib, kind, sample, threads):
-        k, v = sample[0].copy(), sample[1].copy()
+    def cpu_prep(self, sample):
+        return sample[0].copy(), sample[1].copy()
+
+    def cpu_sort(self, lib, kind, work, threads):
+        k, v = work
         if kind == "reference":
             rc = lib.keyvalue_qsort(7, 6, k.ctypes.data, v.ctypes.data, k.size, 0, 0)
         else:
             rc = lib.keyvalue_qsort_mt(7, 6, k.ctypes.data, v.ctypes.data, k.size, 0, 0, threads)
         assert rc == 0
+
+    def cpu_run(self, lib, kind, sample, threads):
+        self.cpu_sort(lib, kind, self.cpu_prep(sample), threads)
 
 
 class QsortF32(Workload):
@@ -261,13 +280,19 @@ class QsortF32(Workload):
     def cpu_sample(self, m):
         return (np.random.default_rng(0).random(m, dtype=np.float32) * 2 - 1,)
 
-    def cpu_run(self, lib, kind, sample, threads):
-        k = sample[0].copy()
+    def cpu_prep(self, sample):
+        return (sample[0].copy(),)
+
+    def cpu_sort(self, lib, kind, work, threads):
+        k = work[0]
         if kind == "reference":
             rc = lib.qsort(5, k.ctypes.data, k.size, 0, 0)
         else:
             rc = lib.qsort_mt(5, k.ctypes.data, k.size, 0, 0, threads)
         assert rc == 0
+
+    def cpu_run(self, lib, kind, sample, threads):
+        self.cpu_sort(lib, kind, self.cpu_prep(sample), threads)
 
 
 class SegmentedSort(Workload):
@@ -337,6 +362,39 @@ class SegmentedSort(Workload):
         self.xss.gpu_segmented_sort_percall(self.kdt, "uint32", self.k.data_ptr(),
                                             self.v.data_ptr(), self.off,
                                             stream=self.stream.cuda_stream)
+
+    def percall_leg(self, segments):
+        """The same batch by one single-array call per segment, over the first
+        `segments` segments (0: all).  Segment sizes are drawn i.i.d., so a
+        contiguous block is a uniform sample; its time is scaled by the segment
+        count.  The sampled segments' outputs must equal the batched outputs
+        (this runs after check(), on the batched result of the last step)."""
+        t = self.torch
+        total = int(self.sizes.size)
+        S = total if not segments else min(int(segments), total)
+        e = int(self.off[S])
+        ref_k, ref_v = self.k[:e].clone(), self.v[:e].clone()
+        times = []
+        for _ in range(2):           # the first run is the warm-up
+            with t.cuda.stream(self.stream):
+                self.k[:e].copy_(self.k0[:e])
+                self.v[:e].copy_(self.v0[:e])
+            e0, e1 = t.cuda.Event(enable_timing=True), t.cuda.Event(enable_timing=True)
+            e0.record(self.stream)
+            self.xss.gpu_segmented_sort_percall(self.kdt, "uint32", self.k.data_ptr(),
+                                                self.v.data_ptr(), self.off[:S + 1],
+                                                stream=self.stream.cuda_stream)
+            e1.record(self.stream)
+            e1.synchronize()
+            times.append(e0.elapsed_time(e1))
+        self.xss.stream_status(self.stream.cuda_stream)
+        same = bool((self.k[:e] == ref_k).all()) and bool((self.v[:e] == ref_v).all())
+        del ref_k, ref_v
+        return {"ms_sampled": times[-1], "segments_sampled": S, "segments": total,
+                "keys_sampled": e, "ms_scaled": times[-1] * total / S,
+                "sample": "contiguous block of the i.i.d. segments, time scaled by segment count"
+                          if S < total else "every segment",
+                "identical_outputs": same}
 
     def check(self, samples=300):
         rng = np.random.default_rng(11)
@@ -1078,14 +1136,41 @@ def cpu_baseline(wl, budget_s=12.0, sample_n=1 << 24):
                       f"median of {len(times)} runs"}
 
 
+# The reference's own numbers for these workloads, measured while surveying it
+# (built from its sources with g++ 13.3, AVX-512 dispatch, OpenMP on 8 threads of
+# an x86 Xeon @ 2.70 GHz; single wall-clock runs).  Its SIMD code needs x86-64
+# and its sources do not travel with this repository, so on other hosts the
+# reference arm times the oracle's port and reports these beside it.
+SURVEY_REFERENCE = {
+    "keyvalue_qsort": {"value": 0.1175, "unit": "Gkeys/s", "n": 1 << 28,
+                       "what": "keyvalue_qsort<int64,uint64> ascending, 2^28 in 2.28 s"},
+    "argsort_i64": {"value": 0.0225, "unit": "Gkeys/s", "n": 1 << 28,
+                    "what": "argsort<int64> ascending, 2^28 in 11.9 s"},
+    "qsort_f32": {"value": 0.492, "unit": "Gkeys/s", "n": 1 << 26,
+                  "what": "qsort<float> U[-1,1), 2^26 in 136 ms"},
+    "qsort_f32_2e20": {"value": 0.721, "unit": "Gkeys/s", "n": 1 << 20,
+                       "what": "qsort<float> U[-1,1), 2^20 in 1.45 ms"},
+    "argsort_f64": {"value": 0.0031, "unit": "Gkeys/s", "n": 1 << 24,
+                    "what": "argsort<double> hasnan descending 1% NaN (scalar fallback), "
+                            "2^24 in 5.39 s"},
+}
+SURVEY_HOST = "x86 survey container: 8 threads (OpenMP), Intel Xeon @ 2.70 GHz, AVX-512"
+
+
 def reference_arm(args):
-    """--impl reference: the reference's CPU path on bounded samples of the workload."""
+    """--impl reference: the reference's CPU path on the workload, timed on the
+    host cores.  Where one step at the full size fits the time budget
+    (--ref-budget-s for all timed steps, estimated from a timed sample) every
+    timed step sorts the whole workload; otherwise a bounded sample.  Inputs
+    are restored outside the timed region where the workload separates the
+    copy from the sort (cpu_prep / cpu_sort)."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
     import torch  # noqa: F401  (only for the workload class' sample helpers)
     cls, n_full = WORKLOADS[args.workload]
     wl = cls(None, None, n_full, None)
+    n_full = wl.n
     if hasattr(wl, "default_k"):
         wl.k = args.k if args.k is not None else wl.default_k
     from oracle import pyoracle
@@ -1093,18 +1178,41 @@ def reference_arm(args):
     if lib is None:
         lib, kind = pyoracle.oracle(), "port"
     threads = pyoracle.oracle().max_threads()
-    m = args.cpu_sample
-    wl._cpu_m = m
+    split = hasattr(wl, "cpu_sort")
+
+    def timed(sample, m):
+        wl._cpu_m = m
+        if split:
+            work = wl.cpu_prep(sample)
+            t0 = time.perf_counter()
+            r = wl.cpu_sort(lib, kind, work, threads)
+            return time.perf_counter() - t0, r
+        t0 = time.perf_counter()
+        r = wl.cpu_run(lib, kind, sample, threads)
+        return time.perf_counter() - t0, r
+
+    m = min(args.cpu_sample, n_full)
     sample = wl.cpu_sample(m)
-    for _ in range(args.warmup):
-        wl.cpu_run(lib, kind, sample, threads)
-    t0 = time.perf_counter()
+    t_m = 0.0
+    for _ in range(max(args.warmup, 1)):     # (at least one run for the estimate)
+        t_m, _ = timed(sample, m)
+    if split and m < n_full and not args.ref_sample_only:
+        # n log n growth from the sample to the full size
+        est = t_m * (n_full / m) * (np.log2(n_full) / np.log2(m))
+        if est * args.steps <= args.ref_budget_s:
+            m = n_full
+            sample = wl.cpu_sample(m)
+    dt = 0.0
     done = 0
     for _ in range(args.steps):
-        r = wl.cpu_run(lib, kind, sample, threads)
+        t, r = timed(sample, m)
+        dt += t
         done += r if isinstance(r, int) else m
-    dt = time.perf_counter() - t0
     val = done / dt / 1e9
+    cores = threads if kind == "port" else min(16, os.cpu_count() or 1)
+    label = ("the oracle's task-parallel port of the reference's OpenMP quicksort "
+             "(the reference's SIMD paths need x86-64)" if kind == "port"
+             else "the reference library built from its sources")
     line = {"impl": "reference", "metric": "Gkeys/s", "value": val, "unit": "Gkeys/s",
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": dt / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
@@ -1112,12 +1220,21 @@ def reference_arm(args):
             "dtype": DTYPE_OF[args.workload],
             "data": "synthetic",
             "config": {**wl.describe(), "parallelism": "replicas x1",
-                       "reference_sample": f"bounded CPU sample of {m} keys per step"},
-            "cpu_baseline": {"value": val, "unit": "Gkeys/s",
-                             "cores": threads if kind == "port" else min(16, os.cpu_count() or 1),
-                             "kind": kind, "sample": f"{m} keys per step"},
+                       "reference_sample": ("the full workload per step" if m == n_full
+                                            else f"bounded CPU sample of {m} keys per step"),
+                       "same_config": m == n_full},
+            "cpu_baseline": {"value": val, "unit": "Gkeys/s", "cores": cores, "kind": kind,
+                             "what": label, "host": os.uname().machine,
+                             "sample": f"{m} keys per step",
+                             "input_restore": "outside the timed region" if split
+                                              else "inside the timed region"},
             "e2e": {"value": val, "unit": "Gkeys/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
+    if args.workload in SURVEY_REFERENCE:
+        line["reference_survey_host"] = {**SURVEY_REFERENCE[args.workload],
+                                         "host": SURVEY_HOST,
+                                         "source": "measured while surveying the reference; "
+                                                   "not on this host"}
     print(json.dumps(line), flush=True)
 
 
@@ -1135,7 +1252,7 @@ def replica_throughput(n_per_rank: int, ms_per_step: float, world: int) -> float
     return world * n_per_rank / (ms_per_step / 1e3) / 1e9
 
 
-def run_serving(args):
+def serving_line(args, duration=None):
     """Serving loop under Poisson load (offered 20k req/s by default).
 
     Mix: 45% qsort, 25% argsort, 20% qselect (k uniform in [0, n)), 10%
@@ -1146,7 +1263,7 @@ def run_serving(args):
     request that finds the ring or the server queue full is shed."""
     import torch
     import pyxss as xss
-    torch.cuda.set_device(0)
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
     rng = np.random.default_rng(4)
     nmax = 1 << 26
     dts = ["float32", "int64", "float16", "float64", "uint32"]
@@ -1175,9 +1292,11 @@ def run_serving(args):
     inflight = []            # (ticket, ring_end, bytes_model, check)
     offered = shed_client = submitted = 0
     model_bytes_done = 0
+    clocks = Clocks(int(os.environ.get("LOCAL_RANK", "0")))
     t_start = time.perf_counter()
     t_next = t_start
-    deadline = t_start + args.duration
+    duration = args.duration if duration is None else duration
+    deadline = t_start + duration
     samples = []
     while True:
         now = time.perf_counter()
@@ -1250,6 +1369,7 @@ def run_serving(args):
         assert srv.wait(tk) == 0
         model_bytes_done += mb
     wall = time.perf_counter() - t_start
+    clk = clocks.stop()
     st = srv.stats()
     srv.close()
     shed_total = shed_client + st["shed"]
@@ -1259,7 +1379,7 @@ def run_serving(args):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "mixed",
         "data": "synthetic (seeded Poisson arrivals, seed 4)",
         "config": {"workload": "serving loop", "offered_req_per_s": args.rate,
-                   "duration_s": args.duration, "mix": "45% qsort, 25% argsort, 20% qselect, "
+                   "duration_s": duration, "mix": "45% qsort, 25% argsort, 20% qselect, "
                    "10% keyvalue_qsort", "sizes": "log-uniform [2^10, 2^26]",
                    "dtypes": dts, "hbm_pool_gb": args.serve_budget_gb,
                    "ring_gb": args.ring_gb, "streams": args.serve_streams,
@@ -1274,8 +1394,14 @@ def run_serving(args):
                     "hbm_frac_model": model_bytes_done / wall / 1e9 / peak,
                     "peak_source": peak_src,
                     "checked_samples": len(samples), "checked_ok": all(samples)},
+        "clocks": clk,
+        "checked": bool(samples) and all(samples),
     }
-    print(json.dumps(line), flush=True)
+    return line
+
+
+def run_serving(args):
+    print(json.dumps(serving_line(args)), flush=True)
 
 
 def main():
@@ -1296,10 +1422,21 @@ def main():
     ap.add_argument("--n", type=int, default=0, help="override the array size")
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-sample", type=int, default=1 << 24)
+    ap.add_argument("--ref-budget-s", type=float, default=150.0,
+                    help="reference arm: time budget of the timed steps at the full size")
+    ap.add_argument("--ref-sample-only", action="store_true",
+                    help="reference arm: always time the bounded sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-percall", action="store_true",
                     help="segmented: skip the per-segment-call comparison")
+    ap.add_argument("--percall-segments", type=int, default=20000,
+                    help="segmented: per-call leg over the first N segments, scaled "
+                         "(0: every segment)")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="default workload: skip the f32 / segmented / serving measurements")
+    ap.add_argument("--extras-serving-s", type=float, default=2.0,
+                    help="seconds of arrivals of the serving measurement in the default run")
     args = ap.parse_args()
     assert args.warmup >= 3 or args.impl == "reference", "at least 3 warm-up steps"
 
@@ -1322,8 +1459,33 @@ def main():
 
     import pyxss as xss
     xss.lib()
-    cls, n_full = WORKLOADS[args.workload]
-    n = args.n or n_full
+    ctx = dict(torch=torch, xss=xss, dist=dist, world=world, rank=rank, local=local)
+    res = measure(args, ctx, args.workload, args.n, args.steps, args.warmup,
+                  do_e2e=not args.no_e2e, do_cpu=not args.no_cpu_baseline,
+                  percall_segments=None if args.no_percall else args.percall_segments)
+    extras = None
+    if (args.workload == "keyvalue_qsort" and not args.n and not args.no_extras
+            and world == 1 and rank == 0):
+        extras = measure_extras(args, ctx)
+    if rank == 0:
+        line = res["line"]
+        if extras is not None:
+            line["extras"] = extras
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def measure(args, ctx, workload, n_override, steps, warmup, do_e2e=True, do_cpu=True,
+            percall_segments=None):
+    """One device-resident workload: W untimed warm-up steps, then K steps timed
+    with CUDA events on the launching stream (input restored before each step,
+    outside the events); the slowest rank's time when several ranks run.
+    Returns {"line": the contract's JSON object for this workload}."""
+    torch, xss, dist = ctx["torch"], ctx["xss"], ctx["dist"]
+    world, rank, local = ctx["world"], ctx["rank"], ctx["local"]
+    cls, n_full = WORKLOADS[workload]
+    n = n_override or n_full
     stream = torch.cuda.Stream()
     wl = cls(torch, xss, n, stream)
     n = wl.n
@@ -1341,7 +1503,7 @@ def main():
             dist.barrier()
         torch.cuda.synchronize()
 
-    for _ in range(args.warmup):
+    for _ in range(warmup):
         with torch.cuda.stream(stream):
             wl.restore()
             wl.run()
@@ -1354,7 +1516,7 @@ def main():
     barrier()
     total_ms = 0.0
     t_wall = time.perf_counter()
-    for _ in range(args.steps):
+    for _ in range(steps):
         with torch.cuda.stream(stream):
             wl.restore()
             if flush is not None:
@@ -1375,9 +1537,9 @@ def main():
     for kind in xss.PROF_KINDS:
         k_ms, k_n = xss.prof_read(kind)
         if k_n:
-            kernels[kind] = {"ms_per_step": k_ms / args.steps, "launches_per_step": k_n / args.steps}
+            kernels[kind] = {"ms_per_step": k_ms / steps, "launches_per_step": k_n / steps}
     dom_ms, dom_launches = xss.prof_read(wl.dominant) if wl.dominant else (0.0, 0)
-    dom_steps = args.steps
+    dom_steps = steps
     if dom_launches == 0 and hasattr(wl, "run_nograph"):
         # kernels inside a replayed graph cannot be bracketed by events: time
         # the dominant kernel in one untimed run of the same launch sequence
@@ -1401,26 +1563,13 @@ def main():
     xss.stream_status(stream.cuda_stream)
     checked = wl.check()
     percall = None
-    if hasattr(wl, "run_percall") and not args.no_percall:
-        # the same batch by one single-array call per segment (untimed warm-up first)
-        pc = []
-        for _ in range(2):
-            with torch.cuda.stream(stream):
-                wl.restore()
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            e0.record(stream)
-            with torch.cuda.stream(stream):
-                wl.run_percall()
-            e1.record(stream)
-            e1.synchronize()
-            pc.append(e0.elapsed_time(e1))
-        xss.stream_status(stream.cuda_stream)
-        percall = pc[-1]
+    if hasattr(wl, "run_percall") and percall_segments is not None:
+        percall = wl.percall_leg(percall_segments)
 
     if dist is not None:
         total_ms = max_over_ranks(total_ms, dist, "cuda")
 
-    ms_per_step = total_ms / args.steps
+    ms_per_step = total_ms / steps
     value = replica_throughput(n, ms_per_step, world)
 
     peak, peak_src = _peaks()
@@ -1433,65 +1582,87 @@ def main():
         kernel_name = "select (all kernels of one call)"
         avg_pass_ms = ms_per_step
         achieved = wl.bytes_model() / (ms_per_step / 1e3) / 1e9
-        active = launches / args.steps
-    traffic = _traffic(args.workload, n, n_full)
+        active = launches / steps
+    traffic = _traffic(workload, n, n_full)
 
     e2e = None
-    if not args.no_e2e and rank == 0 and hasattr(wl, "host_run"):
+    if do_e2e and rank == 0 and hasattr(wl, "host_run"):
         wl.host_setup()
         # the same W warm-up steps as the device leg
-        for _ in range(max(args.warmup, 3)):
+        for _ in range(max(warmup, 3)):
             wl.host_restore()
             wl.host_run()
         t = 0.0
-        for _ in range(args.steps):
+        for _ in range(steps):
             wl.host_restore()
             t0 = time.perf_counter()
             wl.host_run()
             t += time.perf_counter() - t0
         bi, bo = wl.host_bytes()
-        e2e = {"value": n * args.steps / t / 1e9, "unit": "Gkeys/s", "h2d_bytes_per_step": bi,
-               "d2h_bytes_per_step": bo, "ms_per_step": t / args.steps * 1e3}
+        e2e = {"value": n * steps / t / 1e9, "unit": "Gkeys/s", "h2d_bytes_per_step": bi,
+               "d2h_bytes_per_step": bo, "ms_per_step": t / steps * 1e3}
 
     cpu = None
-    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+    if rank == 0 and world == 1 and do_cpu:
         cpu = cpu_baseline(wl, sample_n=args.cpu_sample)
 
     # a published reference number for this exact workload (object_point3d only)
     published = (getattr(wl, "published", None) or {}).get(n)
-    if rank == 0:
-        line = {
-            "metric": "Gkeys/s", "value": value, "unit": "Gkeys/s", "n_gpus": world,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
-            "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": value / published if published else None,
-            **({"baseline_published": {"value": published, "unit": "Gkeys/s",
-                                       "source": wl.published_source}} if published else {}),
-            "dtype": DTYPE_OF[args.workload],
-            "data": "synthetic (seeded, generated on device)",
-            "config": {**wl.describe(), "parallelism": f"replicas x{world}"},
-            "roofline": {"bound": "hbm", "kernel": kernel_name,
-                         "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": (achieved / peak) if achieved else None,
-                         "peak_source": peak_src,
-                         "alg_bytes_per_launch": wl.bytes_per_pass(),
-                         "avg_launch_ms": avg_pass_ms, "launches_per_step": active,
-                         "traffic": traffic,
-                         "sort_model_bytes": wl.bytes_model(),
-                         "sort_frac": wl.bytes_model() / (ms_per_step / 1e3) / 1e9 / peak},
-            "e2e": e2e,
-            "cpu_baseline": cpu,
-            "gpu_launches": launches,
-            "kernels": kernels,
-            "clocks": clk,
-            "checked": checked,
-            **({"percall_ms": percall, "speedup_vs_percall": percall / ms_per_step}
-               if percall else {}),
-            "wall_s_timed_region": wall,
-        }
-        print(json.dumps(line), flush=True)
-    if dist is not None:
-        dist.destroy_process_group()
+    line = {
+        "metric": "Gkeys/s", "value": value, "unit": "Gkeys/s", "n_gpus": world,
+        "steps": steps, "warmup": warmup, "ms_per_step": ms_per_step,
+        "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": value / published if published else None,
+        **({"baseline_published": {"value": published, "unit": "Gkeys/s",
+                                   "source": wl.published_source}} if published else {}),
+        "dtype": DTYPE_OF[workload],
+        "data": "synthetic (seeded, generated on device)",
+        "config": {**wl.describe(), "parallelism": f"replicas x{world}"},
+        "roofline": {"bound": "hbm", "kernel": kernel_name,
+                     "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": (achieved / peak) if achieved else None,
+                     "peak_source": peak_src,
+                     "alg_bytes_per_launch": wl.bytes_per_pass(),
+                     "avg_launch_ms": avg_pass_ms, "launches_per_step": active,
+                     "traffic": traffic,
+                     "sort_model_bytes": wl.bytes_model(),
+                     "sort_frac": wl.bytes_model() / (ms_per_step / 1e3) / 1e9 / peak},
+        "e2e": e2e,
+        "cpu_baseline": cpu,
+        "gpu_launches": launches,
+        "kernels": kernels,
+        "clocks": clk,
+        "checked": checked,
+        **({"percall": percall, "speedup_vs_percall": percall["ms_scaled"] / ms_per_step}
+           if percall else {}),
+        "wall_s_timed_region": wall,
+    }
+    wl.release()
+    del wl
+    torch.cuda.synchronize()
+    torch.cuda.empty_cache()
+    return {"line": line}
+
+
+def measure_extras(args, ctx):
+    """The other parts of the headline metric, each measured in the same run
+    with its own clock record and check: float32 qsort at 2^28 (Gkeys/s and %
+    of the HBM roofline), the literal config-4 batch against per-segment calls
+    of the plain GPU sort (per-call leg over a contiguous sample of the
+    segments, scaled by segment count), and a short serving run (p50/p99)."""
+    out = {}
+    steps, warmup = args.steps, max(args.warmup, 3)
+    f32 = measure(args, ctx, "qsort_f32", 0, steps, warmup, do_e2e=False, do_cpu=False)["line"]
+    out["qsort_f32_2e28"] = {k: f32[k] for k in ("value", "unit", "ms_per_step", "roofline",
+                                                 "kernels", "clocks", "checked", "config")}
+    seg_steps = max(3, min(steps, 5))
+    seg = measure(args, ctx, "segmented", 0, seg_steps, 3, do_e2e=False, do_cpu=False,
+                  percall_segments=args.percall_segments)["line"]
+    out["segmented_config4"] = {k: seg.get(k) for k in (
+        "value", "unit", "ms_per_step", "steps", "percall", "speedup_vs_percall", "roofline",
+        "clocks", "checked", "config")}
+    out["serving"] = serving_line(args, duration=args.extras_serving_s)
+    return out
 
 
 if __name__ == "__main__":

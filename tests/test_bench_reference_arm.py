@@ -22,7 +22,7 @@ KEYS = {"impl", "metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_
 def test_reference_arm_runs(workload):
     r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference",
                         "--workload", workload, "--steps", "1", "--warmup", "0",
-                        "--cpu-sample", "20000"],
+                        "--cpu-sample", "20000", "--ref-sample-only"],
                        cwd=ROOT, stdout=subprocess.PIPE, stderr=subprocess.PIPE, text=True,
                        timeout=600)
     assert r.returncode == 0, r.stderr[-2000:]
@@ -41,3 +41,18 @@ def test_published_baseline_only_for_its_workload():
     for name, (c, n_full) in bench.WORKLOADS.items():
         if name != "object_point3d":
             assert not getattr(c, "published", None), name
+
+
+def test_reference_arm_times_the_full_workload_when_it_fits():
+    """A workload that fits the budget is timed at its full size (same_config)."""
+    r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference",
+                        "--workload", "qsort_f32_2e20", "--steps", "2", "--warmup", "1",
+                        "--cpu-sample", "65536"],
+                       cwd=ROOT, stdout=subprocess.PIPE, stderr=subprocess.PIPE, text=True,
+                       timeout=600)
+    assert r.returncode == 0, r.stderr[-2000:]
+    line = json.loads(r.stdout.strip().splitlines()[-1])
+    assert line["config"]["same_config"] is True
+    assert line["cpu_baseline"]["sample"] == f"{1 << 20} keys per step"
+    assert line["cpu_baseline"]["input_restore"] == "outside the timed region"
+    assert line["reference_survey_host"]["value"] > 0
