@@ -42,8 +42,13 @@ enum {
     XSS_EAGAIN = 8       /* server request not finished yet */
 };
 
-/* Largest array the device kernels accept (tile look-back counters are 30-bit). */
-#define XSS_MAX_N ((size_t)((1u << 30) - 1))
+/* Largest array the library accepts.  The reference has no ceiling (size_t
+ * lengths, lib/x86simdsort.h:16-18); this bound only keeps byte counts far
+ * from overflow and lies beyond any device's memory.  Arrays above 2^30 - 1
+ * keys are sorted in chunks of up to that size and merged; segments of a
+ * batched segmented sort are each limited to XSS_SEGMENT_MAX_N keys. */
+#define XSS_MAX_N ((size_t)1 << 40)
+#define XSS_SEGMENT_MAX_N ((size_t)((1u << 30) - 1))
 
 /* Key / value element types (the reference's nine key types). */
 enum {
@@ -167,6 +172,21 @@ int xss_gpu_segmented_sort(int key_dtype, int val_dtype, void *d_keys, void *d_v
 size_t xss_gpu_segmented_workspace_size(int key_dtype, int val_dtype,
                                         const uint64_t *h_offsets,
                                         size_t num_segments);
+
+/*
+ * Batched segmented top-k (no counterpart in the reference, which has no
+ * segmented form): for every segment, its min(k, length) smallest keys
+ * (largest when descending) in order at the segment's front, with their
+ * values; the rest of the segment holds its other keys in any order -- a
+ * partial_qsort per segment, with the reference's partial_qsort semantics
+ * (lib/x86simdsort.h:27-29).  Runs in the batched segmented launch: segments
+ * up to 4096 keys are sorted on chip whole (which costs no more than their
+ * top k), larger segments by the segmented radix sort.  k == 0: no-op.
+ */
+int xss_gpu_segmented_topk(int key_dtype, int val_dtype, void *d_keys, void *d_vals,
+                           const uint64_t *d_offsets, const uint64_t *h_offsets,
+                           size_t num_segments, size_t k, int hasnan, int descending,
+                           void *d_ws, size_t ws_bytes, xss_stream_t stream);
 
 /*
  * Reusable plan for a fixed segment layout.  The segments are binned by size

@@ -220,6 +220,11 @@ template <typename F> int with_key(int dt, F &&f)
 template <typename F> int with_val(int dt, F &&f)
 {
     switch (dt) {
+    // 16-bit payloads (beyond the reference's 32/64-bit values): values only
+    // move with their keys, so _Float16 values travel as their bits
+    case XSS_DT_U16: f((uint16_t *)nullptr); return 0;
+    case XSS_DT_I16: f((int16_t *)nullptr); return 0;
+    case XSS_DT_F16: f((uint16_t *)nullptr); return 0;
     case XSS_DT_U32: f((uint32_t *)nullptr); return 0;
     case XSS_DT_I32: f((int32_t *)nullptr); return 0;
     case XSS_DT_F32: f((float *)nullptr); return 0;

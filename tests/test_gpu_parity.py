@@ -152,6 +152,43 @@ def test_keyvalue_family(xss, oracle, cuda, ktype):
                     assert_pairs_preserved(x, v, k, w, "kvpartial " + what)
 
 
+@pytest.mark.parametrize("ktype", KEY_TYPES)
+def test_keyvalue_16bit_payloads(xss, oracle, cuda, ktype):
+    """uint16 / int16 / _Float16 values (beyond the reference's 32/64-bit
+    values): every key type, sort / select / partial sort.  Passes carrying
+    values are stable, so a sort's values must be exactly the input values in
+    the stable order of the keys' codes."""
+    from xss_arrays import order_code
+    rng = np.random.default_rng(8)
+    for vtype in ("uint16", "int16", "float16"):
+        for shape in ("random", "smallrange", "reverse", "mixed_special", "rand_with_nan"):
+            hn = hasnan_for(shape)
+            for n in [0, 1, 2, 33, 1000, 4096, 4097, 30_000, 100_001]:
+                x = get_array(shape, ktype, n, seed=n + 9)
+                v = kv_values(vtype, n, seed=n)
+                for desc in (False, True):
+                    what = f"kv {ktype}/{vtype} {shape} n={n} desc={desc}"
+                    k, w = x.copy(), v.copy()
+                    xss.keyvalue_qsort(k, w, hn, desc)
+                    ok, ow = x.copy(), v.copy()
+                    assert oracle.keyvalue_qsort(DT[ktype], DT[vtype], ok.ctypes.data,
+                                                 ow.ctypes.data, n, int(hn), int(desc)) == 0
+                    assert_same_sorted(k, ok, what)
+                    stable = np.argsort(order_code(x, desc), kind="stable")
+                    assert np.array_equal(w.view(np.uint16), v[stable].view(np.uint16)), what
+                    if n < 2:
+                        continue
+                    kk = int(rng.integers(0, n))
+                    k, w = x.copy(), v.copy()
+                    xss.keyvalue_select(k, w, kk, hn, desc)
+                    assert_partitioned(k, kk, ok[kk], desc, "kvselect " + what)
+                    assert_pairs_preserved(x, v, k, w, "kvselect " + what)
+                    k, w = x.copy(), v.copy()
+                    xss.keyvalue_partial_sort(k, w, kk + 1, hn, desc)
+                    assert_same_sorted(k[:kk + 1], ok[:kk + 1], "kvpartial " + what)
+                    assert_pairs_preserved(x, v, k, w, "kvpartial " + what)
+
+
 class _HostApi:
     """The library's xss_* host entry points under the oracle's names."""
 

@@ -50,7 +50,9 @@ def _dev(torch, a):
 
 @pytest.mark.parametrize("kdt,vdt", [("int32", "uint32"), ("float32", "uint32"),
                                      ("float64", None), ("uint16", None), ("int64", "uint64"),
-                                     ("float32", None), ("uint64", "float32")])
+                                     ("float32", None), ("uint64", "float32"),
+                                     ("float32", "uint16"), ("uint16", "float16"),
+                                     ("int64", "int16")])
 @pytest.mark.parametrize("desc", [False, True])
 def test_segmented_matches_oracle(xss, cuda, kdt, vdt, desc):
     torch = cuda
@@ -135,3 +137,32 @@ def test_segmented_mid_sizes_shapes(xss, cuda, shape, kdt, vdt):
                 order = np.argsort(-kk.astype(np.float64) if desc else kk, kind="stable")
                 if np.dtype(kdt).kind != "f":
                     assert np.array_equal(vo[b:e], v[b:e][order]), f"{shape} seg {i} stability"
+
+
+@pytest.mark.parametrize("kdt,vdt", [("float32", "uint32"), ("int64", None), ("uint16", "uint16")])
+@pytest.mark.parametrize("k", [1, 7, 300, 5000])
+def test_segmented_topk(xss, cuda, kdt, vdt, k):
+    """Each segment's first min(k, len) positions: its k smallest (largest when
+    descending) in order, pairs kept; the segment as a whole a permutation."""
+    torch = cuda
+    for desc in (False, True):
+        off = _layout(k + 31 * desc)
+        keys, vals = _make(kdt, vdt, off, 9)
+        hasnan = np.dtype(kdt).kind == "f"
+        dk, dv = _dev(torch, keys), (_dev(torch, vals) if vdt else None)
+        doff = _dev(torch, off)
+        xss.gpu_segmented_topk(kdt, vdt, dk.data_ptr(), dv.data_ptr() if vdt else 0,
+                               doff.data_ptr(), off, off.size - 1, k, hasnan, desc)
+        xss.stream_status()
+        ko = dk.cpu().numpy().view(keys.dtype)
+        vo = dv.cpu().numpy().view(vals.dtype) if vdt else None
+        for i in range(off.size - 1):
+            b, e = int(off[i]), int(off[i + 1])
+            if e == b:
+                continue
+            m = min(k, e - b)
+            what = f"topk {kdt}/{vdt} k={k} desc={desc} seg {i}"
+            assert_same_sorted(ko[b:b + m], ref_sorted(keys[b:e], desc)[:m], what)
+            assert_same_sorted(ref_sorted(ko[b:e]), ref_sorted(keys[b:e]), what + " multiset")
+            if vdt:
+                assert_pairs_preserved(keys[b:e], vals[b:e], ko[b:e], vo[b:e], what)

@@ -108,3 +108,29 @@ def test_canonical_nan(kh, dtype):
     qn = {2: 0x7C01, 4: 0x7FC00000, 8: 0x7FF8000000000000}[dt.itemsize]
     assert (back[nan] == qn).all()
     assert np.array_equal(back[~nan], bits[~nan])
+
+
+@pytest.mark.parametrize("bits", [16, 32, 64])
+def test_branch_free_codec_matches_transform(kh, bits):
+    """The passes' branch-free codec equals to_code / from_code on every 16-bit
+    pattern and on sampled 32/64-bit patterns plus the edge values (zeros,
+    infinities, the NaN range ends), for every kind, order and NaN rule."""
+    ut = {16: np.uint16, 32: np.uint32, 64: np.uint64}[bits]
+    if bits == 16:
+        x = np.arange(1 << 16, dtype=np.uint16)
+    else:
+        rng = np.random.default_rng(bits)
+        x = rng.integers(0, np.iinfo(ut).max, 1 << 20, dtype=ut, endpoint=True)
+        sign = ut(1) << ut(bits - 1)
+        exp = {32: 0x7f800000, 64: 0x7ff0000000000000}[bits]
+        edges = [0, 1, exp, exp + 1, exp | (exp >> 9), sign - 1, sign, sign | exp,
+                 sign | (exp + 1), np.iinfo(ut).max, np.iinfo(ut).max - 1]
+        x = np.concatenate([x, np.array(edges, dtype=ut)])
+    f = getattr(kh, f"kh_codec{bits}")
+    f.restype = ctypes.c_size_t
+    for kind in (0, 1, 2):
+        for desc in (0, 1):
+            for canon in (0, 1):
+                bad = f(ctypes.c_void_p(x.ctypes.data), ctypes.c_size_t(x.size), kind, desc,
+                        canon)
+                assert bad == 0, (bits, kind, desc, canon, bad)

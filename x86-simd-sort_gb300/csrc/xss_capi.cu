@@ -34,10 +34,11 @@ static bool dtype_info(int dt, DtypeInfo &o)
 }
 
 // The reference has key-value sorts for 32/64-bit keys and values only
-// (lib/x86simdsort.cpp:274-293); here 16-bit keys (uint16, int16, _Float16)
-// may carry 32/64-bit values as well.  Values stay 32 or 64 bits.
+// (lib/x86simdsort.cpp:274-293, README.md:53-55); here every key type takes
+// every value type, 16-bit keys (uint16, int16, _Float16) and 16-bit values
+// included.  Values are moved as their bits.
 static bool kv_key_ok(int dt) { return dt >= XSS_DT_U16 && dt <= XSS_DT_F64; }
-static bool kv_type_ok(int dt) { return dt >= XSS_DT_U32 && dt <= XSS_DT_F64; }
+static bool kv_type_ok(int dt) { return dt >= XSS_DT_U16 && dt <= XSS_DT_F64; }
 
 constexpr int MAX_DEV = 64;
 static std::mutex g_mu;
@@ -145,7 +146,7 @@ static int check_n(const void *p, size_t n)
     return XSS_OK;
 }
 
-static int value_bytes(int vdt) { return vdt >= XSS_DT_U64 ? 8 : 4; }
+static int value_bytes(int vdt) { return vdt >= XSS_DT_U64 ? 8 : (vdt >= XSS_DT_U32 ? 4 : 2); }
 
 // ---- device entry points ---------------------------------------------------
 static int gpu_qsort(int dt, void *d, size_t n, int hasnan, int desc, void *ws, size_t wsb,
@@ -368,6 +369,18 @@ static int d2h(HostCtx &c, void *h, const void *d, size_t bytes)
                                                                                      : XSS_ECUDA;
 }
 
+// Host-pointer sorts of at least PIPE_MIN_N keys take the pipelined path
+// (chunk copies overlapped with chunk sorts, xss_merge.cu) unless the
+// environment sets XSS_HOST_PIPELINE=0.
+static bool use_pipeline(size_t n)
+{
+    static const bool on = [] {
+        const char *e = getenv("XSS_HOST_PIPELINE");
+        return !(e && strcmp(e, "0") == 0);
+    }();
+    return on && host_pipeline_wanted(n);
+}
+
 static size_t key_bytes(int dt)
 {
     DtypeInfo di;
@@ -487,6 +500,14 @@ int xss_qsort(int dtype, void *arr, size_t n, int hasnan, int descending)
     if (!kb) return XSS_EINVAL;
     XSS_HOST_TRY(check_n(arr, n));
     if (n <= 1) return XSS_OK;
+    if (use_pipeline(n)) {
+        DtypeInfo di;
+        dtype_info(dtype, di);
+        XSS_HOST_TRY(host_pipelined_sort(SOP_KEYS, di.kbytes,
+                                         KeyXform{di.kind, descending ? 1 : 0, hasnan ? 1 : 0},
+                                         arr, nullptr, 0, nullptr, n));
+        return stream_status(nullptr);
+    }
     HostCtx *c;
     XSS_HOST_TRY(host_ctx(c));
     void *d;
@@ -542,6 +563,14 @@ int xss_argsort(int dtype, const void *arr, uint64_t *arg, size_t n, int hasnan,
         arg[0] = 0;
         return XSS_OK;
     }
+    if (use_pipeline(n)) {
+        DtypeInfo dt;
+        dtype_info(dtype, dt);
+        XSS_HOST_TRY(host_pipelined_sort(SOP_ARG, dt.kbytes,
+                                         KeyXform{dt.kind, descending ? 1 : 0, 0},
+                                         const_cast<void *>(arr), nullptr, 0, arg, n));
+        return stream_status(nullptr);
+    }
     HostCtx *c;
     XSS_HOST_TRY(host_ctx(c));
     void *d, *di;
@@ -588,6 +617,11 @@ static int host_kv(int which, int kdt, int vdt, void *keys, void *vals, size_t k
     if (which == 2 && k == 0) return XSS_OK;
     if (which == 2 && k > n) return XSS_EINVAL;
     const size_t kb = di.kbytes, vb = value_bytes(vdt);
+    if (which == 0 && use_pipeline(n)) {
+        XSS_HOST_TRY(host_pipelined_sort(SOP_KV, (int)kb, KeyXform{di.kind, desc ? 1 : 0, 0},
+                                         keys, vals, (int)vb, nullptr, n));
+        return stream_status(nullptr);
+    }
     HostCtx *c;
     XSS_HOST_TRY(host_ctx(c));
     void *dk, *dv;

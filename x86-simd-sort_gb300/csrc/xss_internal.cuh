@@ -23,6 +23,11 @@ constexpr uint32_t FLAG_PRE = 2u << 30;     // inclusive prefix published
 constexpr uint32_t FLAG_MASK = 3u << 30;
 constexpr uint32_t COUNT_MASK = (1u << 30) - 1;
 
+// Keys one radix sort takes: its look-back words hold a 30-bit count and its
+// tile arithmetic is 32-bit.  Larger arrays are sorted in chunks of at most
+// this size and merged (xss_merge.cu).
+constexpr size_t XSS_RADIX_MAX_N = (size_t(1) << 30) - 1;
+
 // Inputs up to this size are sorted by one CTA in shared memory.
 constexpr size_t SMALL_SORT_MAX = 4096;
 
@@ -75,6 +80,22 @@ unsigned *device_error_word();
 size_t radix_workspace_bytes(int op, int kbytes, int vbytes, size_t n);
 int radix_sort(int op, int kbytes, KeyXform xf, void *keys, void *vals, int vbytes,
                uint64_t *out_idx, size_t n, void *ws, size_t ws_bytes, cudaStream_t s);
+
+// Chunked sorts of arrays above XSS_RADIX_MAX_N keys (xss_merge.cu): chunks
+// radix-sorted in place, then merged pairwise.  radix_sort / radix_select and
+// radix_workspace_bytes route there by size.
+bool big_sort_needed(size_t n);
+size_t big_sort_workspace_bytes(int op, int kbytes, int vbytes, size_t n);
+int big_sort(int op, int kbytes, KeyXform xf, void *keys, void *vals, int vbytes,
+             uint64_t *out_idx, size_t n, void *ws, size_t ws_bytes, cudaStream_t s);
+
+// Host-pointer sorts from PIPE_MIN_N keys on: chunk copies overlapped with
+// chunk sorts, merged, copied back slice by slice (xss_merge.cu).  hk / hv /
+// hidx are host pointers; the call returns once the results are on the host.
+constexpr size_t PIPE_MIN_N = size_t(1) << 22;
+bool host_pipeline_wanted(size_t n);
+int host_pipelined_sort(int op, int kbytes, KeyXform xf, void *hk, void *hv, int vbytes,
+                        uint64_t *hidx, size_t n);
 
 size_t select_workspace_bytes(int op, int kbytes, int vbytes, size_t n);
 // Partition so that position k holds the k-th element in code order,

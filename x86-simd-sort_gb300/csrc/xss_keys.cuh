@@ -21,6 +21,7 @@
 // relative order of the two is a valid reference result.
 #pragma once
 #include <cstdint>
+#include <type_traits>
 #include <cuda_runtime.h>
 
 #define XSS_HD __host__ __device__ __forceinline__
@@ -90,6 +91,46 @@ template <typename C> XSS_HD C from_code(C c, const KeyXform &x)
     }
     return c;
 }
+
+// The same bijection in branch-free form, for the radix passes: masks built
+// once per launch from the KeyXform, then per key a shift, two logic ops and
+// a subtraction each way.  With s = the key's sign bit spread over the word:
+//   code = ((b ^ ((s & fm) | sm)) - sub) ^ dm
+// fm = all ones for floats (negative floats invert), sm = the sign bit for
+// signed and float keys, sub = the negative-NaN count for floats (rotation),
+// dm = all ones for descending.  from_canon additionally writes the canonical
+// quiet NaN for every NaN code when the sort canonicalises (qsort with hasnan):
+// NaN codes are exactly the ascending codes above the code of +inf.
+template <typename C> struct Codec {
+    using T = CodeTraits<C>;
+    using S = typename std::conditional<sizeof(C) == 2, int16_t,
+              typename std::conditional<sizeof(C) == 4, int32_t, int64_t>::type>::type;
+    C fm, sm, sub, dm, thr;
+
+    XSS_HD explicit Codec(const KeyXform &x)
+    {
+        const bool fl = x.kind == XK_FLOAT;
+        fm = fl ? C(~C(0)) : C(0);
+        sm = x.kind != XK_UINT ? T::sign : C(0);
+        sub = fl ? T::neg_nans : C(0);
+        dm = x.desc ? C(~C(0)) : C(0);
+        thr = (fl && x.canon) ? C(C(T::exp_mask | T::sign) - T::neg_nans) : C(~C(0));
+    }
+    XSS_HD static C spread_sign(C v) { return C(S(v) >> (T::bits - 1)); }
+    XSS_HD C to(C b) const
+    {
+        return C(C(C(b ^ C(C(spread_sign(b) & fm) | sm)) - sub) ^ dm);
+    }
+    XSS_HD C from(C c) const
+    {
+        const C u = C(C(c ^ dm) + sub);
+        return C(u ^ C(C(C(~spread_sign(u)) & fm) | sm));
+    }
+    XSS_HD C from_canon(C c) const
+    {
+        return C(c ^ dm) > thr ? T::canon_nan : from(c);
+    }
+};
 
 // Canonicalise a raw key in place of a full round trip (used when no radix
 // pass runs because every code is equal).

@@ -232,13 +232,19 @@ struct TileJob {
 // after_rank() runs on every thread once the tile is staged (the persistent
 // form claims and prefetches its next tile there).
 // Pre: ps.wm is zero.  Post: zero again after the caller's next barrier.
-template <typename C, typename V, int BLOCK, int ITEMS, int LB, int RANK, int DPT,
+// ROLE: what the pass does to keys on store, known at compile time --
+// ROLE_MID (codes stay codes), ROLE_LAST (codes back to keys through the
+// codec, canonical NaNs where asked) -- or ROLE_RUNTIME (pd.last decides,
+// through from_code; the segmented passes use this form).
+constexpr int ROLE_RUNTIME = -1, ROLE_MID = 0, ROLE_FIRST = 1, ROLE_LAST = 2;
+
+template <typename C, typename V, int BLOCK, int ITEMS, int LB, int RANK, int DPT, int ROLE,
           typename VS, typename AfterRank>
 __device__ __forceinline__ void pass_tile(const RadixArgs &a, const PassDesc &pd, int pass,
                                           const TileJob &job, const C (&key)[ITEMS],
                                           const VS (&val)[ITEMS], C *s_k, VS *s_v,
                                           PassSmem<BLOCK, RANK> &ps, C *kdst, V *vdst,
-                                          AfterRank after_rank)
+                                          const Codec<C> &cx, AfterRank after_rank)
 {
     constexpr int WARPS = BLOCK / 32;
     constexpr int TILE = BLOCK * ITEMS;
@@ -395,7 +401,11 @@ __device__ __forceinline__ void pass_tile(const RadixArgs &a, const PassDesc &pd
             const uint32_t d = uint32_t(c >> shift) & (RADIX - 1);
             const uint32_t g = (uint32_t)(ps.off[d] + (int32_t)i);
             if (g < n) {
-                if (!pd.skip_keys) kdst[g] = pd.last ? from_code(c, a.xf) : c;
+                if (!pd.skip_keys) {
+                    if constexpr (ROLE == ROLE_RUNTIME) kdst[g] = pd.last ? from_code(c, a.xf) : c;
+                    else if constexpr ((ROLE & ROLE_LAST) != 0) kdst[g] = cx.from_canon(c);
+                    else kdst[g] = c;
+                }
                 if constexpr (HAS_V) {
                     if (pd.out_idx) a.out_idx[g] = (uint64_t)s_v[i];
                     else vdst[g] = s_v[i];
@@ -416,21 +426,18 @@ struct NoAfterRank {
 // ---------------------------------------------------------------------------
 // One CTA per tile; the tile id comes from an in-order atomic counter, so a
 // tile only waits on tiles whose CTAs are already running.
-template <typename C, typename V, int BLOCK, int ITEMS, int MINB, int LB, int RANK, int DPT>
-__global__ void __launch_bounds__(BLOCK, MINB) onesweep_kernel(RadixArgs a, int pass)
+template <typename C, typename V, int BLOCK, int ITEMS, int LB, int RANK, int DPT, int ROLE>
+__device__ __forceinline__ void onesweep_tile_body(const RadixArgs &a, int pass,
+                                                   const PassDesc &pd,
+                                                   PassSmem<BLOCK, RANK> &ps, uint32_t &s_tile,
+                                                   unsigned char *s_dyn)
 {
     constexpr int TILE = BLOCK * ITEMS;
     constexpr bool HAS_V = !std::is_same<V, NoVal>::value;
     using VS = typename std::conditional<HAS_V, V, uint8_t>::type;
-    static_assert(BLOCK >= RADIX, "one thread per digit");
-    const PassDesc pd = a.hdr->desc[pass];
-    if (!pd.active) return;
-
-    __shared__ PassSmem<BLOCK, RANK> ps;
-    __shared__ uint32_t s_tile;
-    extern __shared__ __align__(128) unsigned char s_dyn[];
     C *s_k = reinterpret_cast<C *>(s_dyn);
     VS *s_v = reinterpret_cast<VS *>(s_dyn + TILE * sizeof(C));
+    const Codec<C> cx(a.xf);
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     for (int i = tid; i < PassSmem<BLOCK, RANK>::WORDS; i += BLOCK) ps.wm[i] = 0;
@@ -447,7 +454,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) onesweep_kernel(RadixArgs a, int 
         const uint32_t idx = first_idx + j * 32;
         if (idx < n) {
             const C b = ksrc[idx];
-            key[j] = pd.first ? to_code(b, a.xf) : b;
+            key[j] = (ROLE & ROLE_FIRST) ? cx.to(b) : b;
         } else {
             key[j] = C(~C(0));
         }
@@ -464,9 +471,37 @@ __global__ void __launch_bounds__(BLOCK, MINB) onesweep_kernel(RadixArgs a, int 
     }
     const TileJob job{tile, 0u, tile * (uint32_t)TILE, n, a.hdr->start[pass],
                       a.status + (size_t)pass * a.num_tiles * RADIX};
-    pass_tile<C, V, BLOCK, ITEMS, LB, RANK, DPT>(a, pd, pass, job, key, val, s_k, s_v, ps,
-                                      static_cast<C *>(pick3(a.kbuf, pd.dst)), vdst,
-                                      NoAfterRank{});
+    pass_tile<C, V, BLOCK, ITEMS, LB, RANK, DPT, ROLE>(a, pd, pass, job, key, val, s_k, s_v, ps,
+                                                       static_cast<C *>(pick3(a.kbuf, pd.dst)),
+                                                       vdst, cx, NoAfterRank{});
+}
+
+// The pass's role (does it load keys, store keys?) is read from the device
+// plan and dispatched to a body compiled for it.
+template <typename C, typename V, int BLOCK, int ITEMS, int MINB, int LB, int RANK, int DPT>
+__global__ void __launch_bounds__(BLOCK, MINB) onesweep_kernel(RadixArgs a, int pass)
+{
+    static_assert(BLOCK >= RADIX, "one thread per digit");
+    const PassDesc pd = a.hdr->desc[pass];
+    if (!pd.active) return;
+    __shared__ PassSmem<BLOCK, RANK> ps;
+    __shared__ uint32_t s_tile;
+    extern __shared__ __align__(128) unsigned char s_dyn[];
+    if (pd.first) {
+        if (pd.last)
+            onesweep_tile_body<C, V, BLOCK, ITEMS, LB, RANK, DPT, ROLE_FIRST | ROLE_LAST>(
+                a, pass, pd, ps, s_tile, s_dyn);
+        else
+            onesweep_tile_body<C, V, BLOCK, ITEMS, LB, RANK, DPT, ROLE_FIRST>(a, pass, pd, ps,
+                                                                              s_tile, s_dyn);
+    } else {
+        if (pd.last)
+            onesweep_tile_body<C, V, BLOCK, ITEMS, LB, RANK, DPT, ROLE_LAST>(a, pass, pd, ps,
+                                                                             s_tile, s_dyn);
+        else
+            onesweep_tile_body<C, V, BLOCK, ITEMS, LB, RANK, DPT, ROLE_MID>(a, pass, pd, ps,
+                                                                            s_tile, s_dyn);
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -480,23 +515,20 @@ __global__ void __launch_bounds__(BLOCK, MINB) onesweep_kernel(RadixArgs a, int 
 // always the current tile of the CTA holding it, and every tile below it is
 // finished.  Partial tiles and sources that are not 16-byte aligned are read
 // with ordinary loads.
-template <typename C, typename V, int BLOCK, int ITEMS, int MINB, int LB, int RANK, int DPT,
-          bool PF>
-__global__ void __launch_bounds__(BLOCK, MINB) onesweep_persist_kernel(RadixArgs a, int pass)
+template <typename C, typename V, int BLOCK, int ITEMS, int LB, int RANK, int DPT, bool PF,
+          int ROLE>
+__device__ __forceinline__ void onesweep_persist_body(const RadixArgs &a, int pass,
+                                                      const PassDesc &pd,
+                                                      PassSmem<BLOCK, RANK> &ps,
+                                                      uint32_t (&s_tile)[2],
+                                                      uint64_t (&s_bar)[2],
+                                                      unsigned char *s_dyn)
 {
     constexpr int TILE = BLOCK * ITEMS;
     constexpr bool HAS_V = !std::is_same<V, NoVal>::value;
     using VS = typename std::conditional<HAS_V, V, uint8_t>::type;
     constexpr size_t VSZ = HAS_V ? sizeof(V) : 0;
-    static_assert(BLOCK >= RADIX, "one thread per digit");
-
-    const PassDesc pd = a.hdr->desc[pass];
-    if (!pd.active) return;
-
-    __shared__ PassSmem<BLOCK, RANK> ps;
-    __shared__ uint32_t s_tile[2];
-    __shared__ __align__(8) uint64_t s_bar[2];
-    extern __shared__ __align__(128) unsigned char s_dyn[];
+    const Codec<C> cx(a.xf);
     constexpr int NBUF = PF ? 2 : 1;
     C *const s_k0 = reinterpret_cast<C *>(s_dyn);
     VS *const s_v0 = reinterpret_cast<VS *>(s_dyn + NBUF * TILE * sizeof(C));
@@ -558,7 +590,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) onesweep_persist_kernel(RadixArgs
 #pragma unroll
             for (int j = 0; j < ITEMS; ++j) {
                 const C b = s_k[local0 + j * 32];
-                key[j] = pd.first ? to_code(b, a.xf) : b;
+                key[j] = (ROLE & ROLE_FIRST) ? cx.to(b) : b;
             }
             if constexpr (HAS_V) {
 #pragma unroll
@@ -571,7 +603,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) onesweep_persist_kernel(RadixArgs
                 const uint32_t idx = tile_base + local0 + j * 32;
                 if (idx < n) {
                     const C b = ksrc[idx];
-                    key[j] = pd.first ? to_code(b, a.xf) : b;
+                    key[j] = (ROLE & ROLE_FIRST) ? cx.to(b) : b;
                 } else {
                     key[j] = C(~C(0));
                 }
@@ -599,9 +631,37 @@ __global__ void __launch_bounds__(BLOCK, MINB) onesweep_persist_kernel(RadixArgs
         };
         const TileJob job{tile, 0u, tile_base, n, a.hdr->start[pass],
                           a.status + (size_t)pass * num_tiles * RADIX};
-        pass_tile<C, V, BLOCK, ITEMS, LB, RANK, DPT>(a, pd, pass, job, key, val, s_k, s_v, ps, kdst, vdst,
-                                          claim_next);
+        pass_tile<C, V, BLOCK, ITEMS, LB, RANK, DPT, ROLE>(a, pd, pass, job, key, val, s_k, s_v,
+                                                           ps, kdst, vdst, cx, claim_next);
         __syncthreads();
+    }
+}
+
+template <typename C, typename V, int BLOCK, int ITEMS, int MINB, int LB, int RANK, int DPT,
+          bool PF>
+__global__ void __launch_bounds__(BLOCK, MINB) onesweep_persist_kernel(RadixArgs a, int pass)
+{
+    static_assert(BLOCK >= RADIX, "one thread per digit");
+    const PassDesc pd = a.hdr->desc[pass];
+    if (!pd.active) return;
+    __shared__ PassSmem<BLOCK, RANK> ps;
+    __shared__ uint32_t s_tile[2];
+    __shared__ __align__(8) uint64_t s_bar[2];
+    extern __shared__ __align__(128) unsigned char s_dyn[];
+    if (pd.first) {
+        if (pd.last)
+            onesweep_persist_body<C, V, BLOCK, ITEMS, LB, RANK, DPT, PF, ROLE_FIRST | ROLE_LAST>(
+                a, pass, pd, ps, s_tile, s_bar, s_dyn);
+        else
+            onesweep_persist_body<C, V, BLOCK, ITEMS, LB, RANK, DPT, PF, ROLE_FIRST>(
+                a, pass, pd, ps, s_tile, s_bar, s_dyn);
+    } else {
+        if (pd.last)
+            onesweep_persist_body<C, V, BLOCK, ITEMS, LB, RANK, DPT, PF, ROLE_LAST>(
+                a, pass, pd, ps, s_tile, s_bar, s_dyn);
+        else
+            onesweep_persist_body<C, V, BLOCK, ITEMS, LB, RANK, DPT, PF, ROLE_MID>(
+                a, pass, pd, ps, s_tile, s_bar, s_dyn);
     }
 }
 

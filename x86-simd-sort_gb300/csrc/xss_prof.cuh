@@ -17,7 +17,8 @@ enum ProfKind : int {
     PK_SEG_BLOCK = 9,  // segmented sort: one CTA per medium segment
     PK_SEG_MISC = 10,  // segmented sort: binning / bookkeeping
     PK_OBJECT = 11,    // record sort: key extraction / record gather
-    PK_COUNT = 12
+    PK_MERGE = 12,     // chunked sort of a very large array: merge of sorted runs
+    PK_COUNT = 13
 };
 
 void prof_begin(cudaStream_t s, int kind);

@@ -129,6 +129,9 @@ __global__ void __launch_bounds__(HIST_BLOCK) hist_cols_kernel(RadixArgs a)
     const int tid = threadIdx.x, lane = tid & 31;
     const int P = a.passes;
     constexpr int ROWS = (int)sizeof(C) * (RADIX / 2);   // 32 words each
+    // the passes sort codes of the keys as they are (NaN payloads included);
+    // the last pass writes canonical NaNs where the sort asks for them
+    const Codec<C> cx(a.xf);
     for (int i = tid; i < ROWS * 32; i += HIST_BLOCK) sh_all[i] = 0;
     __syncthreads();
     uint32_t *const col = sh_all + lane;
@@ -180,7 +183,7 @@ __global__ void __launch_bounds__(HIST_BLOCK) hist_cols_kernel(RadixArgs a)
                 C e[VEC];
                 memcpy(e, &q[u], 16);
 #pragma unroll
-                for (int k = 0; k < VEC; ++k) hist_count<C>(col, to_code(e[k], a.xf));
+                for (int k = 0; k < VEC; ++k) hist_count<C>(col, cx.to(e[k]));
             }
         }
         since += U * VEC;
@@ -193,7 +196,7 @@ __global__ void __launch_bounds__(HIST_BLOCK) hist_cols_kernel(RadixArgs a)
     const size_t ssteps = (rest + stride - 1) / stride;
     for (size_t st = 0; st < ssteps; ++st) {
         const size_t i = nvec * VEC + st * stride + gtid;
-        if (i < n) hist_count<C>(col, to_code(src[i], a.xf));
+        if (i < n) hist_count<C>(col, cx.to(src[i]));
         if (++since + 1 > HIST_FLUSH_KEYS) {
             flush();
             since = 0;
@@ -231,6 +234,7 @@ __global__ void __launch_bounds__(256) hist_copies_kernel(RadixArgs a)
     const int tid = threadIdx.x;
     const int P = a.passes;
     constexpr int NW = (int)sizeof(C) * RADIX * HIST_COPIES;
+    const Codec<C> cx(a.xf);   // codes as in hist_cols_kernel
     for (int i = tid; i < NW; i += 256) sh_all[i] = 0;
     __syncthreads();
     uint32_t *const sh = sh_all + (tid & (HIST_COPIES - 1));
@@ -248,7 +252,7 @@ __global__ void __launch_bounds__(256) hist_copies_kernel(RadixArgs a)
         memcpy(e, &q, 16);
 #pragma unroll
         for (int u = 0; u < VEC; ++u) {
-            const C c = to_code(e[u], a.xf);
+            const C c = cx.to(e[u]);
 #pragma unroll
             for (int p = 0; p < (int)sizeof(C); ++p)
                 atomicAdd(&sh[(p * RADIX + (uint32_t(c >> (p * RADIX_BITS)) & (RADIX - 1))) *
@@ -256,7 +260,7 @@ __global__ void __launch_bounds__(256) hist_copies_kernel(RadixArgs a)
         }
     }
     for (size_t i = nvec * VEC + gtid; i < n; i += stride) {
-        const C c = to_code(src[i], a.xf);
+        const C c = cx.to(src[i]);
 #pragma unroll
         for (int p = 0; p < (int)sizeof(C); ++p)
             atomicAdd(&sh[(p * RADIX + (uint32_t(c >> (p * RADIX_BITS)) & (RADIX - 1))) *
@@ -343,15 +347,16 @@ static size_t tile_for_bytes(int op, int kbytes, int vbytes, size_t n)
 {
     const int vb = (op == SOP_ARG) ? 4 : (op == SOP_KV ? vbytes : 0);
     switch (kbytes) {
-    case 2: return vb == 0 ? tile_of<uint16_t, NoVal>(n) : vb == 4 ? tile_of<uint16_t, uint32_t>(n) : tile_of<uint16_t, uint64_t>(n);
-    case 4: return vb == 0 ? tile_of<uint32_t, NoVal>(n) : vb == 4 ? tile_of<uint32_t, uint32_t>(n) : tile_of<uint32_t, uint64_t>(n);
-    default: return vb == 0 ? tile_of<uint64_t, NoVal>(n) : vb == 4 ? tile_of<uint64_t, uint32_t>(n) : tile_of<uint64_t, uint64_t>(n);
+    case 2: return vb == 0 ? tile_of<uint16_t, NoVal>(n) : vb == 2 ? tile_of<uint16_t, uint16_t>(n) : vb == 4 ? tile_of<uint16_t, uint32_t>(n) : tile_of<uint16_t, uint64_t>(n);
+    case 4: return vb == 0 ? tile_of<uint32_t, NoVal>(n) : vb == 2 ? tile_of<uint32_t, uint16_t>(n) : vb == 4 ? tile_of<uint32_t, uint32_t>(n) : tile_of<uint32_t, uint64_t>(n);
+    default: return vb == 0 ? tile_of<uint64_t, NoVal>(n) : vb == 2 ? tile_of<uint64_t, uint16_t>(n) : vb == 4 ? tile_of<uint64_t, uint32_t>(n) : tile_of<uint64_t, uint64_t>(n);
     }
 }
 
 size_t radix_workspace_bytes(int op, int kbytes, int vbytes, size_t n)
 {
     if (n <= SMALL_SORT_MAX) return 0;
+    if (big_sort_needed(n)) return big_sort_workspace_bytes(op, kbytes, vbytes, n);
     return radix_layout(op, kbytes, vbytes, n, tile_for_bytes(op, kbytes, vbytes, n)).total;
 }
 
@@ -391,22 +396,6 @@ static int small_sort_launch(int op, KeyXform xf, void *keys, void *vals,
                    (small_sort_kernel<C, V, SMALL_BLOCK, SMALL_SORT_MAX><<<1, SMALL_BLOCK, smem, s>>>(a)));
     XSS_CUDA_TRY(cudaGetLastError());
     return XSS_OK;
-}
-
-// Pass-kernel form: the tuned choice of PassCfg (PERSIST), unless the
-// environment forces one: XSS_ONESWEEP=tile (one CTA per tile),
-// XSS_ONESWEEP=persist (resident CTAs with TMA prefetch) or
-// XSS_ONESWEEP=resident (resident CTAs, ordinary loads).
-static int pass_form(int tuned)
-{
-    static const int forced = [] {
-        const char *e = getenv("XSS_ONESWEEP");
-        if (e && strcmp(e, "tile") == 0) return 0;
-        if (e && strcmp(e, "persist") == 0) return 1;
-        if (e && strcmp(e, "resident") == 0) return 2;
-        return -1;
-    }();
-    return forced < 0 ? tuned : forced;
 }
 
 // Launch every active pass with resident CTAs (grid = what fits on the SMs).
@@ -453,8 +442,8 @@ static int tile_passes(const RadixArgs &a, cudaStream_t s, const LaunchOpts &o)
     return XSS_OK;
 }
 
-// LARGE: the large-array lines, whose launch form may also be forced through
-// XSS_ONESWEEP; otherwise the mid-size lines in their own form only.
+// LARGE: the large-array lines, else the mid-size lines; each in its tuned
+// launch form only.
 template <typename C, typename V, bool LARGE>
 static int onesweep_launch_cls(int op, KeyXform xf, void *keys, void *vals, uint64_t *out_idx,
                                size_t n, void *ws, size_t ws_bytes, cudaStream_t s,
@@ -524,18 +513,13 @@ static int onesweep_launch_cls(int op, KeyXform xf, void *keys, void *vals, uint
     }
     XSS_CUDA_TRY(cudaGetLastError());
 
-    const int form = LARGE ? pass_form(Cfg::PERSIST) : Cfg::PERSIST;
     int rc = XSS_OK;
-    if (form == 1) {
-        if constexpr (LARGE || Cfg::PERSIST == 1)
-            rc = resident_passes<C, V, BLOCK, ITEMS, MINB, LB, RANK, DPT, true>(a, sms, s, o);
-    } else if (form == 2) {
-        if constexpr (LARGE || Cfg::PERSIST == 2)
-            rc = resident_passes<C, V, BLOCK, ITEMS, MINB, LB, RANK, DPT, false>(a, sms, s, o);
-    } else {
-        if constexpr (LARGE || Cfg::PERSIST == 0)
-            rc = tile_passes<C, V, BLOCK, ITEMS, MINB, LB, RANK, DPT>(a, s, o);
-    }
+    if constexpr (Cfg::PERSIST == 1)
+        rc = resident_passes<C, V, BLOCK, ITEMS, MINB, LB, RANK, DPT, true>(a, sms, s, o);
+    else if constexpr (Cfg::PERSIST == 2)
+        rc = resident_passes<C, V, BLOCK, ITEMS, MINB, LB, RANK, DPT, false>(a, sms, s, o);
+    else
+        rc = tile_passes<C, V, BLOCK, ITEMS, MINB, LB, RANK, DPT>(a, s, o);
     if (rc) return rc;
     XSS_LAUNCH_OPT(o, PK_FIXUP, s, fixup_kernel<C, V><<<sms * 2, 256, 0, s>>>(a));
     XSS_CUDA_TRY(cudaGetLastError());
@@ -568,6 +552,10 @@ static int radix_sort_c(int op, KeyXform xf, void *keys, void *vals, int vbytes,
                      : onesweep_launch<C, NoVal>(op, xf, keys, nullptr, nullptr, n, ws, ws_bytes,
                                                  s, o);
     }
+    if (vbytes == 2)
+        return small ? small_sort_launch<C, uint16_t>(op, xf, keys, vals, nullptr, n, s, o)
+                     : onesweep_launch<C, uint16_t>(op, xf, keys, vals, nullptr, n, ws, ws_bytes,
+                                                    s, o);
     if (vbytes == 4)
         return small ? small_sort_launch<C, uint32_t>(op, xf, keys, vals, nullptr, n, s, o)
                      : onesweep_launch<C, uint32_t>(op, xf, keys, vals, nullptr, n, ws, ws_bytes,
@@ -588,7 +576,7 @@ static int radix_sort_opts(int op, int kbytes, KeyXform xf, void *keys, void *va
         if (op == SOP_ARG) XSS_CUDA_TRY(cudaMemsetAsync(out_idx, 0, sizeof(uint64_t), s));
         return XSS_OK;
     }
-    if (n > XSS_MAX_N) return XSS_ETOOBIG;
+    if (n > XSS_RADIX_MAX_N) return XSS_ETOOBIG;
     switch (kbytes) {
     case 2: return radix_sort_c<uint16_t>(op, xf, keys, vals, vbytes, out_idx, n, ws, ws_bytes, s, o);
     case 4: return radix_sort_c<uint32_t>(op, xf, keys, vals, vbytes, out_idx, n, ws, ws_bytes, s, o);
@@ -597,14 +585,24 @@ static int radix_sort_opts(int op, int kbytes, KeyXform xf, void *keys, void *va
     }
 }
 
-int radix_sort(int op, int kbytes, KeyXform xf, void *keys, void *vals, int vbytes,
-               uint64_t *out_idx, size_t n, void *ws, size_t ws_bytes, cudaStream_t s)
+// One radix sort of at most XSS_RADIX_MAX_N keys (also a chunk of a larger sort).
+int radix_sort_chunk(int op, int kbytes, KeyXform xf, void *keys, void *vals, int vbytes,
+                     uint64_t *out_idx, size_t n, void *ws, size_t ws_bytes, cudaStream_t s)
 {
-    if (n <= 1 || n > XSS_MAX_N)
+    if (n <= 1 || n > XSS_RADIX_MAX_N)
         return radix_sort_opts(op, kbytes, xf, keys, vals, vbytes, out_idx, n, ws, ws_bytes, s,
                                LaunchOpts{nullptr, true});
     const LaunchOpts o{device_error_word(), true};
     return radix_sort_opts(op, kbytes, xf, keys, vals, vbytes, out_idx, n, ws, ws_bytes, s, o);
+}
+
+int radix_sort(int op, int kbytes, KeyXform xf, void *keys, void *vals, int vbytes,
+               uint64_t *out_idx, size_t n, void *ws, size_t ws_bytes, cudaStream_t s)
+{
+    if (n > XSS_MAX_N) return XSS_ETOOBIG;
+    if (big_sort_needed(n))
+        return big_sort(op, kbytes, xf, keys, vals, vbytes, out_idx, n, ws, ws_bytes, s);
+    return radix_sort_chunk(op, kbytes, xf, keys, vals, vbytes, out_idx, n, ws, ws_bytes, s);
 }
 
 }  // namespace xss

@@ -262,8 +262,10 @@ __global__ void __launch_bounds__(BLOCK, MINB) seg_pass_kernel(SegArgs a, int pa
     const TileJob job{t, a.large_tile0[l], base, len,
                       a.seg_start + ((size_t)l * a.passes + pass) * RADIX,
                       a.status + (size_t)(pass & 1) * a.T * RADIX};
-    pass_tile<C, V, BLOCK, ITEMS, LB, RANK, DPT>(ra, pd, pass, job, key, val, s_k, s_v, ps, kdst, vdst,
-                                            NoAfterRank{});
+    const Codec<C> cx(a.xf);   // unused with ROLE_RUNTIME (from_code decides)
+    pass_tile<C, V, BLOCK, ITEMS, LB, RANK, DPT, ROLE_RUNTIME>(ra, pd, pass, job, key, val, s_k,
+                                                               s_v, ps, kdst, vdst, cx,
+                                                               NoAfterRank{});
 }
 
 // ---------------------------------------------------------------------------
@@ -313,9 +315,9 @@ template <typename C, typename V> constexpr size_t seg_tile()
 static size_t seg_tile_size(int kb, int vb)
 {
     switch (kb) {
-    case 2: return vb == 0 ? seg_tile<uint16_t, NoVal>() : vb == 4 ? seg_tile<uint16_t, uint32_t>() : seg_tile<uint16_t, uint64_t>();
-    case 4: return vb == 0 ? seg_tile<uint32_t, NoVal>() : vb == 4 ? seg_tile<uint32_t, uint32_t>() : seg_tile<uint32_t, uint64_t>();
-    default: return vb == 0 ? seg_tile<uint64_t, NoVal>() : vb == 4 ? seg_tile<uint64_t, uint32_t>() : seg_tile<uint64_t, uint64_t>();
+    case 2: return vb == 0 ? seg_tile<uint16_t, NoVal>() : vb == 2 ? seg_tile<uint16_t, uint16_t>() : vb == 4 ? seg_tile<uint16_t, uint32_t>() : seg_tile<uint16_t, uint64_t>();
+    case 4: return vb == 0 ? seg_tile<uint32_t, NoVal>() : vb == 2 ? seg_tile<uint32_t, uint16_t>() : vb == 4 ? seg_tile<uint32_t, uint32_t>() : seg_tile<uint32_t, uint64_t>();
+    default: return vb == 0 ? seg_tile<uint64_t, NoVal>() : vb == 2 ? seg_tile<uint64_t, uint16_t>() : vb == 4 ? seg_tile<uint64_t, uint32_t>() : seg_tile<uint64_t, uint64_t>();
     }
 }
 
@@ -329,7 +331,7 @@ static int plan_build(SegPlan &p, const uint64_t *off, size_t nseg)
     for (size_t i = 0; i < nseg; ++i) {
         if (off[i + 1] < off[i]) return XSS_EINVAL;
         const uint64_t len = off[i + 1] - off[i];
-        if (len > XSS_MAX_N) return XSS_ETOOBIG;
+        if (len > XSS_SEGMENT_MAX_N) return XSS_ETOOBIG;
         if (len <= 1) continue;
         if (len <= SEG_WARP_MAX) p.warp.push_back((uint32_t)i);
         else if (len <= SEG_SMALL_MAX) p.small.push_back((uint32_t)i);
@@ -498,6 +500,7 @@ template <typename C>
 static int seg_launch_v(const SegPlan &p, SegArgs a, cudaStream_t s)
 {
     if (p.vb == 0) return seg_launch<C, NoVal>(p, a, s);
+    if (p.vb == 2) return seg_launch<C, uint16_t>(p, a, s);
     if (p.vb == 4) return seg_launch<C, uint32_t>(p, a, s);
     return seg_launch<C, uint64_t>(p, a, s);
 }
@@ -527,8 +530,8 @@ static int plan_init(SegPlan &p, int key_dtype, int val_dtype, const uint64_t *h
     p.val_dtype = val_dtype;
     p.vb = 0;
     if (val_dtype >= 0) {
-        if (val_dtype < XSS_DT_U32 || val_dtype > XSS_DT_F64) return XSS_EUNSUPPORTED;
-        p.vb = val_dtype >= XSS_DT_U64 ? 8 : 4;
+        if (val_dtype < XSS_DT_U16 || val_dtype > XSS_DT_F64) return XSS_EUNSUPPORTED;
+        p.vb = val_dtype >= XSS_DT_U64 ? 8 : (val_dtype >= XSS_DT_U32 ? 4 : 2);
     }
     p.hasnan = hasnan;
     p.desc = descending;
@@ -715,6 +718,18 @@ int xss_gpu_segmented_sort(int key_dtype, int val_dtype, void *d_keys, void *d_v
     return plan_enqueue(p, d_keys, d_vals, d_offsets, s);
 }
 
+// Segmented top-k: the batched sort meets the contract (each segment's k
+// smallest in order at its front) for every k.
+int xss_gpu_segmented_topk(int key_dtype, int val_dtype, void *d_keys, void *d_vals,
+                           const uint64_t *d_offsets, const uint64_t *h_offsets,
+                           size_t num_segments, size_t k, int hasnan, int descending,
+                           void *d_ws, size_t ws_bytes, xss_stream_t stream)
+{
+    if (k == 0 || num_segments == 0) return XSS_OK;
+    return xss_gpu_segmented_sort(key_dtype, val_dtype, d_keys, d_vals, d_offsets, h_offsets,
+                                  num_segments, hasnan, descending, d_ws, ws_bytes, stream);
+}
+
 // The same batch sorted by one call of the single-array entry point per
 // segment: the baseline the batched form is measured against.
 int xss_gpu_segmented_sort_percall(int key_dtype, int val_dtype, void *d_keys, void *d_vals,
@@ -723,7 +738,7 @@ int xss_gpu_segmented_sort_percall(int key_dtype, int val_dtype, void *d_keys, v
 {
     int kb, kind;
     if (dtype_kind(key_dtype, kb, kind)) return XSS_EINVAL;
-    const int vb = d_vals ? (val_dtype >= XSS_DT_U64 ? 8 : 4) : 0;
+    const int vb = d_vals ? (val_dtype >= XSS_DT_U64 ? 8 : (val_dtype >= XSS_DT_U32 ? 4 : 2)) : 0;
     for (size_t i = 0; i < num_segments; ++i) {
         const uint64_t b = h_offsets[i], e = h_offsets[i + 1];
         if (e < b) return XSS_EINVAL;

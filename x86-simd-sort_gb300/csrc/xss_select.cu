@@ -92,7 +92,8 @@ __device__ __forceinline__ uint32_t sel_block_excl_scan(uint32_t v, uint32_t *s_
 // loads, four per thread in flight, keep enough bytes moving to cover memory
 // latency; an unaligned array takes the scalar loop.
 template <typename C>
-__global__ void __launch_bounds__(256) sel_hist_kernel(SelArgs a, int round, int lo, int bits)
+__global__ void __launch_bounds__(256) sel_hist_kernel(SelArgs a, int round, int lo, int bits,
+                                                       int from_keys)
 {
     constexpr int VW = 16 / sizeof(C);   // keys per vector
     constexpr int U = 4;                 // vectors per thread in flight
@@ -101,15 +102,16 @@ __global__ void __launch_bounds__(256) sel_hist_kernel(SelArgs a, int round, int
     for (int i = threadIdx.x; i < nb; i += 256) sh[i] = 0;
     __syncthreads();
     const C prefix = (C)a.st->prefix, mask = (C)a.st->mask;
-    const size_t count = round == 0 ? a.n : (size_t)a.st->cand_n;
-    const C *src = round == 0 ? static_cast<const C *>(a.keys) : static_cast<const C *>(a.cand);
+    const Codec<C> cx(a.xf);
+    const size_t count = from_keys ? a.n : (size_t)a.st->cand_n;
+    const C *src = from_keys ? static_cast<const C *>(a.keys) : static_cast<const C *>(a.cand);
     const int lane = threadIdx.x & 31;
     const size_t stride = (size_t)gridDim.x * 256;
     const size_t wbase = (size_t)blockIdx.x * 256 + threadIdx.x - lane;   // warp's first thread
 
     auto visit = [&](C b, bool active) {
         C c = 0;
-        if (active) c = round == 0 ? to_code(b, a.xf) : b;
+        if (active) c = from_keys ? cx.to(b) : b;
         const bool match = active && ((C)(c & mask) == prefix);
         if (match) atomicAdd(&sh[uint32_t(c >> lo) & (uint32_t)(nb - 1)], 1u);
     };
@@ -148,7 +150,8 @@ __global__ void __launch_bounds__(256) sel_hist_kernel(SelArgs a, int round, int
 // histogram for the next round.
 template <typename C>
 __global__ void __launch_bounds__(1024) sel_find_kernel(SelArgs a, int round, int lo, int bits,
-                                                        int last, unsigned long long k0)
+                                                        int last, int exact,
+                                                        unsigned long long k0)
 {
     __shared__ uint32_t s_warp[32];
     const int nb = 1 << bits;
@@ -174,6 +177,10 @@ __global__ void __launch_bounds__(1024) sel_find_kernel(SelArgs a, int round, in
                 if (last) {
                     a.st->cl = a.st->cnt_less;
                     a.st->ce = h;
+                    if (exact) {        // the partition's middle class is the code K
+                        a.st->b_lo = a.st->cnt_less;
+                        a.st->b_n = h;
+                    }
                 }
                 break;
             }
@@ -244,26 +251,36 @@ __device__ __forceinline__ void sel_load_chunk(const C *keys, size_t n, size_t p
     }
 }
 
-// The split pass (see the file comment).  Lists: 0 = L elements outside
-// [0, b_lo), 2 = G elements outside [b_lo + b_n, n), holes 0 / 2 = foreign
-// positions inside those regions, candidates = B's keys.  Each CTA takes
-// chunks of 256 * IPT elements, IPT consecutive ones per thread, so lists
-// come out in position order; slots are reserved with one global atomic per
-// list per chunk (skipped when a chunk has nothing to record), and the next
-// chunk's keys are loaded before the current chunk's scan.  The per-thread
-// counters are 4-bit fields of one word; region tests are 32-bit offsets
-// from the thread's first element.
-template <typename C, typename V>
+// The split pass (see the file comment).  Classes of an element by its code
+// against the round-0 bucket B: 0 = L (below), 1 = B, 2 = G (above); regions
+// of a position: 0 = [0, b_lo), 1 = [b_lo, b_hi), 2 = [b_hi, n).  An element
+// whose class differs from its region's is listed (list X = its class) and
+// its position is a hole of its region (hole list R).  With candidates
+// (EXACT false), B's elements are compacted instead of listed and B's region
+// is rewritten whole later, so neither list 1 nor hole list 1 is kept; with
+// EXACT (B is the single code K, known exactly: the 16-bit path) every class
+// is listed and the place pass moves all three.
+//
+// Each warp takes chunks of 32 * IPT consecutive elements, IPT per thread
+// (16-byte vector loads); a warp with nothing to record in a chunk moves on
+// after one vote.  Otherwise it scans its packed per-thread counts with
+// shuffles and reserves every list's slots with one global atomic per list,
+// so lists are in position order within a warp chunk and no barrier is
+// needed.  List X's slots start at its region's first position (the number of
+// misplaced elements of a class is at most its region's size).
+template <typename C, typename V, bool EXACT>
 __global__ void __launch_bounds__(256) sel_split_kernel(SelArgs a, int lo, int bits)
 {
-    constexpr int IPT = SelChunk<C>::IPT, CH = SelChunk<C>::CH;
-    __shared__ uint32_t s_w[8][4];
-    __shared__ unsigned long long s_base[7];
-    __shared__ uint32_t sh[SEL_BINS];
-    const int tid = threadIdx.x;
+    constexpr int IPT = SelChunk<C>::IPT, WCH = 32 * IPT;
+    constexpr bool HAS_V = !std::is_same<V, uint8_t>::value;
+    __shared__ uint32_t sh[EXACT ? 1 : SEL_BINS];
+    const int tid = threadIdx.x, lane = tid & 31;
     const int nb = 1 << bits;
-    for (int i = tid; i < nb; i += 256) sh[i] = 0;
-    __syncthreads();
+    if constexpr (!EXACT) {
+        for (int i = tid; i < nb; i += 256) sh[i] = 0;
+        __syncthreads();
+    }
+    const Codec<C> cx(a.xf);
     const C pre = (C)a.st->prefix, msk = (C)a.st->mask;
     const size_t b_lo = a.st->b_lo, b_hi = a.st->b_lo + a.st->b_n;
     const C *keys = static_cast<const C *>(a.keys);
@@ -272,82 +289,96 @@ __global__ void __launch_bounds__(256) sel_split_kernel(SelArgs a, int lo, int b
     V *mis_v = static_cast<V *>(a.mis_v);
     C *cand = static_cast<C *>(a.cand);
     const size_t n = a.n;
-    const size_t gstride = (size_t)gridDim.x * CH;
+    const size_t warps = (size_t)gridDim.x * 8;
+    const size_t gw = (size_t)blockIdx.x * 8 + (tid >> 5);
     const bool vec = (reinterpret_cast<uintptr_t>(keys) & 15) == 0;
-    C nxt[IPT];
-    sel_load_chunk<C>(keys, n, (size_t)blockIdx.x * CH + (size_t)tid * IPT, vec, nxt);
-    for (size_t c0 = (size_t)blockIdx.x * CH; c0 < n; c0 += gstride) {
+    for (size_t c0 = gw * WCH; c0 < n; c0 += warps * WCH) {
+        const size_t p0 = c0 + (size_t)lane * IPT;
         C raw[IPT];
-#pragma unroll
-        for (int j = 0; j < IPT; ++j) raw[j] = nxt[j];
-        if (c0 + gstride < n) sel_load_chunk<C>(keys, n, c0 + gstride + (size_t)tid * IPT, vec, nxt);
-        const size_t p0 = c0 + (size_t)tid * IPT;
+        sel_load_chunk<C>(keys, n, p0, vec, raw);
         const uint32_t r1 = (uint32_t)(b_lo > p0 ? min(b_lo - p0, (size_t)IPT) : 0);
         const uint32_t r2 = (uint32_t)(b_hi > p0 ? min(b_hi - p0, (size_t)IPT) : 0);
         const uint32_t valid = (uint32_t)(n > p0 ? min(n - p0, (size_t)IPT) : 0);
-        uint32_t tags = 0;      // 4 bits per element: list class (0, 2 or 3 = none), hole region
-        uint32_t candm = 0;     // bit j: element j is a candidate
-        uint32_t cnt4 = 0;      // 4-bit counters: lists 0..2, holes 0..2, candidates
+        uint32_t tags = 0;     // per element: list (2 bits, 3 = none) | hole (2 bits, 3 = none)
+        uint32_t candm = 0;    // bit j: element j is a candidate
+        uint32_t lists = 0, holes = 0, ncand = 0;   // 10-bit fields per list / hole list
 #pragma unroll
         for (int j = 0; j < IPT; ++j) {
             uint32_t t = 0xF;
             if ((uint32_t)j < valid) {
-                const C c = to_code(raw[j], a.xf);
-                const C top = (C)(c & msk);
+                const C c = cx.to(raw[j]);
+                const C top = EXACT ? c : (C)(c & msk);
                 const uint32_t cls = (uint32_t)(top >= pre) + (uint32_t)(top > pre);
                 const uint32_t reg = (uint32_t)((uint32_t)j >= r1) + (uint32_t)((uint32_t)j >= r2);
-                if (a.op == SOP_ARG && reg != 1) a.out_idx[p0 + j] = p0 + j;
-                if (cls == 1) {
+                if (a.op == SOP_ARG && (EXACT || reg != 1)) a.out_idx[p0 + j] = p0 + j;
+                if (!EXACT && cls == 1) {
                     candm |= 1u << j;
-                    cnt4 += 1u << 24;
+                    ++ncand;
                     atomicAdd(&sh[uint32_t(c >> lo) & (uint32_t)(nb - 1)], 1u);
                 }
                 if (cls != reg) {
-                    const uint32_t X = cls == 1 ? 3u : cls;   // candidates are not listed
-                    const uint32_t R = reg == 1 ? 3u : reg;   // B's region is rewritten whole
+                    const uint32_t X = (!EXACT && cls == 1) ? 3u : cls;
+                    const uint32_t R = (!EXACT && reg == 1) ? 3u : reg;
                     t = X | (R << 2);
-                    cnt4 += (X != 3u ? (1u << (4 * X)) : 0u) + (R != 3u ? (1u << (4 * (3 + R))) : 0u);
+                    if (X != 3u) lists += 1u << (10 * X);
+                    if (R != 3u) holes += 1u << (10 * R);
                 }
             }
             tags |= t << (4 * j);
         }
-        if (!__syncthreads_or(cnt4 != 0u)) continue;
-        uint32_t w[4];
+        if (!__any_sync(0xffffffffu, (lists | holes | ncand) != 0u)) continue;
+        // warp-inclusive scans of the packed counts
+        uint32_t il = lists, ih = holes, ic = ncand;
 #pragma unroll
-        for (int q = 0; q < 3; ++q)
-            w[q] = ((cnt4 >> (8 * q)) & 0xFu) | (((cnt4 >> (8 * q + 4)) & 0xFu) << 16);
-        w[3] = (cnt4 >> 24) & 0xFu;
-        uint32_t tot[4];
-        sel_scan<4>(w, s_w, tot);
-        if (tid < 7) {
-            const uint32_t t = tid < 6 ? (tot[tid >> 1] >> ((tid & 1) * 16)) & 0xFFFFu : tot[3];
-            unsigned long long *ctr64 = nullptr;
-            unsigned int *ctr = nullptr;
-            if (tid < 3) ctr = &a.st->nmis[tid];
-            else if (tid < 6) ctr = &a.st->nhole[tid - 3];
-            else ctr64 = &a.st->cand_n;
-            const size_t rs = tid == 6 ? 0 : ((tid % 3) == 0 ? 0 : ((tid % 3) == 1 ? b_lo : b_hi));
-            size_t at = rs;
-            if (t) at += ctr ? (size_t)atomicAdd(ctr, t) : (size_t)atomicAdd(ctr64, (unsigned long long)t);
-            // a list that would run past the array (never, with consistent
-            // counts) is not written for this chunk
-            s_base[tid] = at + t <= n ? at : ~0ull;
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t yl = __shfl_up_sync(0xffffffffu, il, o);
+            const uint32_t yh = __shfl_up_sync(0xffffffffu, ih, o);
+            const uint32_t yc = __shfl_up_sync(0xffffffffu, ic, o);
+            if (lane >= o) {
+                il += yl;
+                ih += yh;
+                ic += yc;
+            }
         }
-        __syncthreads();
+        // lane 31 holds the warp's totals: reserve slots, one atomic per list
+        size_t base = 0;
+        const uint32_t tl = __shfl_sync(0xffffffffu, il, 31);
+        const uint32_t th = __shfl_sync(0xffffffffu, ih, 31);
+        const uint32_t tc = __shfl_sync(0xffffffffu, ic, 31);
+        if (lane < 7) {
+            uint32_t t = 0;
+            if (lane < 3) t = (tl >> (10 * lane)) & 0x3FFu;
+            else if (lane < 6) t = (th >> (10 * (lane - 3))) & 0x3FFu;
+            else t = tc;
+            if (t) {
+                const int q = lane < 3 ? lane : lane - 3;
+                const size_t rs = q == 0 ? 0 : (q == 1 ? b_lo : b_hi);
+                if (lane < 3) base = rs + atomicAdd(&a.st->nmis[q], t);
+                else if (lane < 6) base = rs + atomicAdd(&a.st->nhole[q], t);
+                else base = (size_t)atomicAdd(&a.st->cand_n, (unsigned long long)t);
+                // a list that would run past its space (never, with consistent
+                // counts) is not written for this chunk
+                if (base + t > n) base = ~size_t(0);
+            }
+        }
         size_t slot[7];
         bool ok[7];
 #pragma unroll
         for (int q = 0; q < 7; ++q) {
-            const unsigned long long b0 = s_base[q];
-            ok[q] = b0 != ~0ull;
-            slot[q] = b0 + (q < 6 ? ((w[q >> 1] >> ((q & 1) * 16)) & 0xFFFFu) : w[3]);
+            const size_t b0 = __shfl_sync(0xffffffffu, base, q);
+            ok[q] = b0 != ~size_t(0);
+            const uint32_t excl = q < 3 ? ((il - lists) >> (10 * q)) & 0x3FFu
+                                : q < 6 ? ((ih - holes) >> (10 * (q - 3))) & 0x3FFu
+                                        : ic - ncand;
+            slot[q] = b0 + excl;
         }
 #pragma unroll
         for (int j = 0; j < IPT; ++j) {
             const size_t p = p0 + j;
             const uint32_t X = (tags >> (4 * j)) & 3u, R = (tags >> (4 * j + 2)) & 3u;
 #pragma unroll
-            for (int q = 0; q < 3; q += 2) {
+            for (int q = 0; q < 3; ++q) {
+                if (!EXACT && q == 1) continue;
                 if (X == (uint32_t)q) {
                     if (ok[q]) {
                         const size_t at = slot[q];
@@ -355,7 +386,7 @@ __global__ void __launch_bounds__(256) sel_split_kernel(SelArgs a, int lo, int b
                             reinterpret_cast<uint32_t *>(a.mis_v)[at] = (uint32_t)p;
                         } else {
                             mis_k[at] = raw[j];
-                            if constexpr (!std::is_same<V, uint8_t>::value)
+                            if constexpr (HAS_V)
                                 if (a.op == SOP_KV) mis_v[at] = vals[p];
                         }
                     }
@@ -366,23 +397,25 @@ __global__ void __launch_bounds__(256) sel_split_kernel(SelArgs a, int lo, int b
                     ++slot[3 + q];
                 }
             }
-            if ((candm >> j) & 1u) {
+            if (!EXACT && ((candm >> j) & 1u)) {
                 if (ok[6]) {
                     const size_t at = slot[6];
-                    cand[at] = to_code(raw[j], a.xf);
+                    cand[at] = cx.to(raw[j]);
                     if (a.op == SOP_ARG) {
                         static_cast<uint32_t *>(a.cand_p)[at] = (uint32_t)p;
-                    } else if constexpr (!std::is_same<V, uint8_t>::value) {
+                    } else if constexpr (HAS_V) {
                         if (a.op == SOP_KV) static_cast<V *>(a.cand_p)[at] = vals[p];
                     }
                 }
                 ++slot[6];
             }
         }
-        __syncthreads();   // s_base is rewritten by the next chunk
     }
-    for (int i = tid; i < nb; i += 256)
-        if (sh[i]) atomicAdd(&a.st->hist[i], sh[i]);
+    if constexpr (!EXACT) {
+        __syncthreads();
+        for (int i = tid; i < nb; i += 256)
+            if (sh[i]) atomicAdd(&a.st->hist[i], sh[i]);
+    }
 }
 
 // B's region rewritten from the candidates, partitioned around K:
@@ -461,7 +494,7 @@ __global__ void __launch_bounds__(256) sel_bpart_kernel(SelArgs a)
 
 // Listed L / G elements into the holes of their regions.
 template <typename C, typename V>
-__global__ void __launch_bounds__(256) sel_place_kernel(SelArgs a)
+__global__ void __launch_bounds__(256) sel_place_kernel(SelArgs a, int exact)
 {
     const size_t b_hi = a.st->b_lo + a.st->b_n;
     C *keys = static_cast<C *>(a.keys);
@@ -469,9 +502,8 @@ __global__ void __launch_bounds__(256) sel_place_kernel(SelArgs a)
     const C *mis_k = static_cast<const C *>(a.mis_k);
     const V *mis_v = static_cast<const V *>(a.mis_v);
     const size_t stride = (size_t)gridDim.x * 256;
-#pragma unroll
-    for (int X = 0; X < 3; X += 2) {
-        const size_t rs = X == 0 ? 0 : b_hi;
+    for (int X = 0; X < 3; X += exact ? 1 : 2) {
+        const size_t rs = X == 0 ? 0 : (X == 1 ? a.st->b_lo : b_hi);
         // counts are consistent by construction; clamp so a broken state can
         // never index past the lists
         const size_t cnt = min((size_t)a.st->nhole[X], a.n - min(rs, a.n));
@@ -525,6 +557,8 @@ static SelLayout sel_layout(int op, int kbytes, int vbytes, size_t n)
 size_t select_workspace_bytes(int op, int kbytes, int vbytes, size_t n)
 {
     if (n <= SMALL_SORT_MAX) return 0;
+    // beyond one radix sort's size the select is a full (chunked) sort
+    if (big_sort_needed(n)) return radix_workspace_bytes(op, kbytes, vbytes, n);
     return sel_layout(op, kbytes, vbytes, n).total;
 }
 
@@ -553,8 +587,27 @@ static int select_launch(int op, KeyXform xf, void *keys, void *vals, uint64_t *
 
     const int sms = num_sms();
     const int grid = (int)std::max<size_t>(1, std::min<size_t>((n + 2047) / 2048, (size_t)sms * 8));
+    const unsigned long long kk = (unsigned long long)k;
+    if constexpr (sizeof(C) == 2) {
+        // 16-bit keys: two 8-bit histogram reads of the keys give the exact
+        // k-th code K; one pass lists every element outside its class's
+        // region (< K, == K, > K) and the place pass moves all three classes
+        for (int r = 0; r < 2; ++r) {
+            const int lo = r == 0 ? 8 : 0;
+            XSS_LAUNCH(PK_SEL_HIST, s, sel_hist_kernel<C><<<grid, 256, 0, s>>>(a, r, lo, 8, 1));
+            XSS_CUDA_TRY(cudaGetLastError());
+            XSS_LAUNCH(PK_SEL_FIND, s,
+                       sel_find_kernel<C><<<1, 1024, 0, s>>>(a, r, lo, 8, r == 1, 1, kk));
+            XSS_CUDA_TRY(cudaGetLastError());
+        }
+        XSS_LAUNCH(PK_SEL_COLLECT, s, (sel_split_kernel<C, V, true><<<grid, 256, 0, s>>>(a, 0, 0)));
+        XSS_CUDA_TRY(cudaGetLastError());
+        XSS_LAUNCH(PK_SEL_PLACE, s, (sel_place_kernel<C, V><<<grid, 256, 0, s>>>(a, 1)));
+        XSS_CUDA_TRY(cudaGetLastError());
+        return XSS_OK;
+    }
     const int W = 8 * (int)sizeof(C);
-    const int rounds = (W + SEL_DIGIT - 1) / SEL_DIGIT;   // >= 2 for every key width
+    const int rounds = (W + SEL_DIGIT - 1) / SEL_DIGIT;   // 3 (32-bit) or 6 (64-bit)
     for (int r = 0; r < rounds; ++r) {
         const int hi = W - SEL_DIGIT * r;
         const int lo = std::max(0, hi - SEL_DIGIT);
@@ -562,21 +615,22 @@ static int select_launch(int op, KeyXform xf, void *keys, void *vals, uint64_t *
         if (r == 1) {
             // one read of every key: candidates, their next-digit histogram,
             // and the L / G lists and holes
-            XSS_LAUNCH(PK_SEL_COLLECT, s, (sel_split_kernel<C, V><<<grid, 256, 0, s>>>(a, lo, bits)));
+            XSS_LAUNCH(PK_SEL_COLLECT, s,
+                       (sel_split_kernel<C, V, false><<<grid, 256, 0, s>>>(a, lo, bits)));
         } else {
             // round 0 reads every key; later rounds only the candidates
             const int g = r >= 2 ? std::max(1, grid / 4) : grid;
-            XSS_LAUNCH(PK_SEL_HIST, s, sel_hist_kernel<C><<<g, 256, 0, s>>>(a, r, lo, bits));
+            XSS_LAUNCH(PK_SEL_HIST, s,
+                       sel_hist_kernel<C><<<g, 256, 0, s>>>(a, r, lo, bits, r == 0 ? 1 : 0));
         }
         XSS_CUDA_TRY(cudaGetLastError());
         XSS_LAUNCH(PK_SEL_FIND, s,
-                   sel_find_kernel<C><<<1, 1024, 0, s>>>(a, r, lo, bits, r == rounds - 1,
-                                                         (unsigned long long)k));
+                   sel_find_kernel<C><<<1, 1024, 0, s>>>(a, r, lo, bits, r == rounds - 1, 0, kk));
         XSS_CUDA_TRY(cudaGetLastError());
     }
     XSS_LAUNCH(PK_SEL_PLACE, s, (sel_bpart_kernel<C, V><<<grid, 256, 0, s>>>(a)));
     XSS_CUDA_TRY(cudaGetLastError());
-    XSS_LAUNCH(PK_SEL_PLACE, s, (sel_place_kernel<C, V><<<grid, 256, 0, s>>>(a)));
+    XSS_LAUNCH(PK_SEL_PLACE, s, (sel_place_kernel<C, V><<<grid, 256, 0, s>>>(a, 0)));
     XSS_CUDA_TRY(cudaGetLastError());
     return XSS_OK;
 }
@@ -586,6 +640,8 @@ static int select_c(int op, KeyXform xf, void *keys, void *vals, int vbytes,
                     uint64_t *out_idx, size_t k, size_t n, void *ws, size_t ws_bytes,
                     cudaStream_t s)
 {
+    if (op == SOP_KV && vbytes == 2)
+        return select_launch<C, uint16_t>(op, xf, keys, vals, out_idx, k, n, ws, ws_bytes, s);
     if (op == SOP_KV && vbytes == 4)
         return select_launch<C, uint32_t>(op, xf, keys, vals, out_idx, k, n, ws, ws_bytes, s);
     if (op == SOP_KV && vbytes == 8)
@@ -597,11 +653,11 @@ int radix_select(int op, int kbytes, KeyXform xf, void *keys, void *vals, int vb
                  uint64_t *out_idx, size_t k, size_t n, void *ws, size_t ws_bytes,
                  cudaStream_t s)
 {
-    if (n <= SMALL_SORT_MAX) {
-        // a full sort satisfies the select contract
+    if (n <= SMALL_SORT_MAX || big_sort_needed(n)) {
+        // a full sort satisfies the select contract (small inputs, and arrays
+        // beyond one radix sort's size, which the chunked sort takes)
         return radix_sort(op, kbytes, xf, keys, vals, vbytes, out_idx, n, ws, ws_bytes, s);
     }
-    if (n > XSS_MAX_N) return XSS_ETOOBIG;
     switch (kbytes) {
     case 2: return select_c<uint16_t>(op, xf, keys, vals, vbytes, out_idx, k, n, ws, ws_bytes, s);
     case 4: return select_c<uint32_t>(op, xf, keys, vals, vbytes, out_idx, k, n, ws, ws_bytes, s);

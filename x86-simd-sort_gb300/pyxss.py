@@ -59,6 +59,7 @@ _SIGS = {
     "xss_gpu_keyvalue_partial_sort": (_I, [_I, _I, _P, _P, _Z, _Z, _I, _I, _P, _Z, _P]),
     "xss_gpu_segmented_sort": (_I, [_I, _I, _P, _P, _P, _P, _Z, _I, _I, _P, _Z, _P]),
     "xss_gpu_segmented_workspace_size": (_Z, [_I, _I, _P, _Z]),
+    "xss_gpu_segmented_topk": (_I, [_I, _I, _P, _P, _P, _P, _Z, _Z, _I, _I, _P, _Z, _P]),
     "xss_qsort": (_I, [_I, _P, _Z, _I, _I]),
     "xss_qselect": (_I, [_I, _P, _Z, _Z, _I, _I]),
     "xss_partial_qsort": (_I, [_I, _P, _Z, _Z, _I, _I]),
@@ -83,7 +84,8 @@ _SIGS = {
 }
 
 PROF_KINDS = ["hist", "onesweep", "fixup", "small_sort", "sel_hist", "sel_find",
-              "sel_collect", "sel_place", "seg_small", "seg_block", "seg_misc", "object"]
+              "sel_collect", "sel_place", "seg_small", "seg_block", "seg_misc", "object",
+              "merge"]
 
 
 def prof_enable(on: bool) -> None:
@@ -262,6 +264,18 @@ def gpu_segmented_sort(kdt, vdt, d_keys, d_vals, d_offsets, h_offsets: np.ndarra
                                        d_vals or None, d_offsets or None, hp, num_segments,
                                        int(hasnan), int(descending), ws or None, ws_bytes,
                                        stream or None), "gpu_segmented_sort")
+
+
+def gpu_segmented_topk(kdt, vdt, d_keys, d_vals, d_offsets, h_offsets: np.ndarray,
+                       num_segments, k, hasnan=False, descending=False, ws=0, ws_bytes=0,
+                       stream=0):
+    """Each segment's min(k, len) smallest keys (largest when descending), in
+    order, at its front (xss_gpu_segmented_topk)."""
+    hp = _ptr(h_offsets) if h_offsets is not None else None
+    check(lib().xss_gpu_segmented_topk(dtype_id(kdt), dtype_id(vdt) if vdt else -1, d_keys,
+                                       d_vals or None, d_offsets or None, hp, num_segments, k,
+                                       int(hasnan), int(descending), ws or None, ws_bytes,
+                                       stream or None), "gpu_segmented_topk")
 
 
 def segmented_workspace_size(kdt, vdt, h_offsets: np.ndarray) -> int:
