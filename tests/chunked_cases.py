@@ -19,7 +19,7 @@ for p in (HERE, ROOT, os.path.join(ROOT, "x86-simd-sort_gb300")):
 
 from golden_io import DT  # noqa: E402
 from xss_arrays import (KEY_TYPES, KV_TYPES, assert_partitioned, assert_same_sorted,  # noqa: E402
-                        get_array, kv_values, order_code, ref_sorted)
+                        bit_code, get_array, kv_values, ref_sorted)
 
 SHAPES = ["random", "constant", "sorted", "reverse", "smallrange", "rand_with_nan",
           "mixed_special"]
@@ -51,7 +51,7 @@ def main() -> int:
                         assert_same_sorted(got, want, "qsort " + what)
                     except AssertionError as e:
                         fails.append(str(e))
-                    stable = np.argsort(order_code(x, desc), kind="stable")
+                    stable = np.argsort(bit_code(x, desc), kind="stable")
                     arg = xss.argsort(x, hn, desc)
                     check(np.array_equal(arg.astype(np.int64), stable), "argsort " + what)
                     if dtype in KV_TYPES and shape in ("random", "mixed_special", "smallrange"):

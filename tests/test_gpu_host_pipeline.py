@@ -7,7 +7,7 @@ import numpy as np
 import pytest
 
 from golden_io import DT
-from xss_arrays import assert_same_sorted, get_array, order_code
+from xss_arrays import assert_same_sorted, bit_code, get_array
 
 pytestmark = pytest.mark.gpu
 
@@ -57,5 +57,5 @@ def test_qsort_host_pipeline_matches_oracle(xss, oracle, cuda):
 def test_argsort_host_pipeline_is_stable_order(xss, cuda, dtype):
     x = get_array("mixed_special" if dtype == "float64" else "smallrange", dtype, N, seed=22)
     arg = xss.argsort(x, True, True)
-    want = np.argsort(order_code(x, True), kind="stable")
+    want = np.argsort(bit_code(x, True), kind="stable")
     assert np.array_equal(arg.astype(np.int64), want)

@@ -158,7 +158,7 @@ def test_keyvalue_16bit_payloads(xss, oracle, cuda, ktype):
     values): every key type, sort / select / partial sort.  Passes carrying
     values are stable, so a sort's values must be exactly the input values in
     the stable order of the keys' codes."""
-    from xss_arrays import order_code
+    from xss_arrays import bit_code
     rng = np.random.default_rng(8)
     for vtype in ("uint16", "int16", "float16"):
         for shape in ("random", "smallrange", "reverse", "mixed_special", "rand_with_nan"):
@@ -174,7 +174,7 @@ def test_keyvalue_16bit_payloads(xss, oracle, cuda, ktype):
                     assert oracle.keyvalue_qsort(DT[ktype], DT[vtype], ok.ctypes.data,
                                                  ow.ctypes.data, n, int(hn), int(desc)) == 0
                     assert_same_sorted(k, ok, what)
-                    stable = np.argsort(order_code(x, desc), kind="stable")
+                    stable = np.argsort(bit_code(x, desc), kind="stable")
                     assert np.array_equal(w.view(np.uint16), v[stable].view(np.uint16)), what
                     if n < 2:
                         continue

@@ -134,3 +134,14 @@ def test_branch_free_codec_matches_transform(kh, bits):
                 bad = f(ctypes.c_void_p(x.ctypes.data), ctypes.c_size_t(x.size), kind, desc,
                         canon)
                 assert bad == 0, (bits, kind, desc, canon, bad)
+
+
+@pytest.mark.parametrize("dtype", ["float16", "int16", "uint16"])
+def test_bit_code_helper_is_the_library_code(kh, dtype):
+    """The tests' bit_code (exact stable-order checks) equals to_code on every
+    16-bit pattern, ascending and descending."""
+    from xss_arrays import bit_code
+    x = np.arange(1 << 16, dtype=np.uint16).view(dtype)
+    for desc in (0, 1):
+        got = _fwd(kh, x.view(np.uint16), KIND[np.dtype(dtype).kind], desc)
+        assert np.array_equal(got.astype(np.uint64), bit_code(x, bool(desc)))

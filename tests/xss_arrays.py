@@ -162,6 +162,26 @@ def order_code(a: np.ndarray, descending: bool = False) -> np.ndarray:
     return ((~c) & full) if descending else c
 
 
+def bit_code(a: np.ndarray, descending: bool = False) -> np.ndarray:
+    """The library's own sort code of every bit pattern (uint64 for all widths):
+    like order_code but -0.0 before +0.0 and NaNs ordered by their bits (all
+    after +inf), so a stable sort by it is the exact order the library's
+    stable paths (key-value, argsort) produce."""
+    nb = a.itemsize
+    u = np.ascontiguousarray(a).view(UINT[nb]).astype(np.uint64)
+    sign = np.uint64(SIGN[nb])
+    full = np.uint64((1 << (8 * nb)) - 1)
+    if a.dtype.kind == "f":
+        neg = (u & sign) != 0
+        c = np.where(neg, (~u) & full, u | sign)
+        c = (c - np.uint64(NEG_NANS[nb])) & full
+    elif a.dtype.kind == "i":
+        c = u ^ sign
+    else:
+        c = u
+    return ((~c) & full) if descending else c
+
+
 # ---- checkers -------------------------------------------------------------------
 def assert_same_sorted(got: np.ndarray, want: np.ndarray, what: str = "") -> None:
     g, w = canon(got), canon(want)

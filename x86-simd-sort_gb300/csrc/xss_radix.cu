@@ -130,8 +130,9 @@ __global__ void __launch_bounds__(HIST_BLOCK) hist_cols_kernel(RadixArgs a)
     const int P = a.passes;
     constexpr int ROWS = (int)sizeof(C) * (RADIX / 2);   // 32 words each
     // the passes sort codes of the keys as they are (NaN payloads included);
-    // the last pass writes canonical NaNs where the sort asks for them
-    const Codec<C> cx(a.xf);
+    // the last pass writes canonical NaNs where the sort asks for them.  (The
+    // branched transform measured faster here than the passes' codec.)
+    const KeyXform xnc{a.xf.kind, a.xf.desc, 0};
     for (int i = tid; i < ROWS * 32; i += HIST_BLOCK) sh_all[i] = 0;
     __syncthreads();
     uint32_t *const col = sh_all + lane;
@@ -183,7 +184,7 @@ __global__ void __launch_bounds__(HIST_BLOCK) hist_cols_kernel(RadixArgs a)
                 C e[VEC];
                 memcpy(e, &q[u], 16);
 #pragma unroll
-                for (int k = 0; k < VEC; ++k) hist_count<C>(col, cx.to(e[k]));
+                for (int k = 0; k < VEC; ++k) hist_count<C>(col, to_code(e[k], xnc));
             }
         }
         since += U * VEC;
@@ -196,7 +197,7 @@ __global__ void __launch_bounds__(HIST_BLOCK) hist_cols_kernel(RadixArgs a)
     const size_t ssteps = (rest + stride - 1) / stride;
     for (size_t st = 0; st < ssteps; ++st) {
         const size_t i = nvec * VEC + st * stride + gtid;
-        if (i < n) hist_count<C>(col, cx.to(src[i]));
+        if (i < n) hist_count<C>(col, to_code(src[i], xnc));
         if (++since + 1 > HIST_FLUSH_KEYS) {
             flush();
             since = 0;
@@ -234,7 +235,7 @@ __global__ void __launch_bounds__(256) hist_copies_kernel(RadixArgs a)
     const int tid = threadIdx.x;
     const int P = a.passes;
     constexpr int NW = (int)sizeof(C) * RADIX * HIST_COPIES;
-    const Codec<C> cx(a.xf);   // codes as in hist_cols_kernel
+    const KeyXform xnc{a.xf.kind, a.xf.desc, 0};   // codes as in hist_cols_kernel
     for (int i = tid; i < NW; i += 256) sh_all[i] = 0;
     __syncthreads();
     uint32_t *const sh = sh_all + (tid & (HIST_COPIES - 1));
@@ -252,7 +253,7 @@ __global__ void __launch_bounds__(256) hist_copies_kernel(RadixArgs a)
         memcpy(e, &q, 16);
 #pragma unroll
         for (int u = 0; u < VEC; ++u) {
-            const C c = cx.to(e[u]);
+            const C c = to_code(e[u], xnc);
 #pragma unroll
             for (int p = 0; p < (int)sizeof(C); ++p)
                 atomicAdd(&sh[(p * RADIX + (uint32_t(c >> (p * RADIX_BITS)) & (RADIX - 1))) *
@@ -260,7 +261,7 @@ __global__ void __launch_bounds__(256) hist_copies_kernel(RadixArgs a)
         }
     }
     for (size_t i = nvec * VEC + gtid; i < n; i += stride) {
-        const C c = cx.to(src[i]);
+        const C c = to_code(src[i], xnc);
 #pragma unroll
         for (int p = 0; p < (int)sizeof(C); ++p)
             atomicAdd(&sh[(p * RADIX + (uint32_t(c >> (p * RADIX_BITS)) & (RADIX - 1))) *

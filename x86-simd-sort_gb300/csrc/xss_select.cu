@@ -261,17 +261,23 @@ __device__ __forceinline__ void sel_load_chunk(const C *keys, size_t n, size_t p
 // EXACT (B is the single code K, known exactly: the 16-bit path) every class
 // is listed and the place pass moves all three.
 //
-// Each warp takes chunks of 32 * IPT consecutive elements, IPT per thread
-// (16-byte vector loads); a warp with nothing to record in a chunk moves on
-// after one vote.  Otherwise it scans its packed per-thread counts with
-// shuffles and reserves every list's slots with one global atomic per list,
-// so lists are in position order within a warp chunk and no barrier is
-// needed.  List X's slots start at its region's first position (the number of
-// misplaced elements of a class is at most its region's size).
+// Each warp takes super-chunks of S chunks of 32 * IPT consecutive elements,
+// IPT per thread (16-byte vector loads).  It classifies all S chunks first
+// (a 4-bit tag per element kept in registers; a candidate is tagged as list
+// 1, which the candidate form does not keep), and a warp with nothing to
+// record in a super-chunk moves on after one vote.  Otherwise it scans its
+// per-thread counts with shuffles and reserves every list's slots with one
+// global atomic per list -- S chunks per reservation keep the contention on
+// the few list counters low -- then reloads the chunks holding records
+// (still in L2) and writes them, so lists are in position order within a
+// super-chunk and no barrier is needed.  List X's slots start at its
+// region's first position (the number of misplaced elements of a class is at
+// most its region's size).  Keys-only exact partitions list no element equal
+// to K: the place pass writes K into the holes of K's region instead.
 template <typename C, typename V, bool EXACT>
 __global__ void __launch_bounds__(256) sel_split_kernel(SelArgs a, int lo, int bits)
 {
-    constexpr int IPT = SelChunk<C>::IPT, WCH = 32 * IPT;
+    constexpr int IPT = SelChunk<C>::IPT, WCH = 32 * IPT, S = 8;
     constexpr bool HAS_V = !std::is_same<V, uint8_t>::value;
     __shared__ uint32_t sh[EXACT ? 1 : SEL_BINS];
     const int tid = threadIdx.x, lane = tid & 31;
@@ -292,47 +298,58 @@ __global__ void __launch_bounds__(256) sel_split_kernel(SelArgs a, int lo, int b
     const size_t warps = (size_t)gridDim.x * 8;
     const size_t gw = (size_t)blockIdx.x * 8 + (tid >> 5);
     const bool vec = (reinterpret_cast<uintptr_t>(keys) & 15) == 0;
-    for (size_t c0 = gw * WCH; c0 < n; c0 += warps * WCH) {
-        const size_t p0 = c0 + (size_t)lane * IPT;
-        C raw[IPT];
-        sel_load_chunk<C>(keys, n, p0, vec, raw);
-        const uint32_t r1 = (uint32_t)(b_lo > p0 ? min(b_lo - p0, (size_t)IPT) : 0);
-        const uint32_t r2 = (uint32_t)(b_hi > p0 ? min(b_hi - p0, (size_t)IPT) : 0);
-        const uint32_t valid = (uint32_t)(n > p0 ? min(n - p0, (size_t)IPT) : 0);
-        uint32_t tags = 0;     // per element: list (2 bits, 3 = none) | hole (2 bits, 3 = none)
-        uint32_t candm = 0;    // bit j: element j is a candidate
-        uint32_t lists = 0, holes = 0, ncand = 0;   // 10-bit fields per list / hole list
+    const bool keys_only_exact = EXACT && a.op == SOP_KEYS;
+    for (size_t s0 = gw * (S * WCH); s0 < n; s0 += warps * (S * WCH)) {
+        uint32_t tags[S];
+        unsigned long long lists = 0, holes = 0;   // 16-bit fields per list / hole list
+        uint32_t ncand = 0;
 #pragma unroll
-        for (int j = 0; j < IPT; ++j) {
-            uint32_t t = 0xF;
-            if ((uint32_t)j < valid) {
-                const C c = cx.to(raw[j]);
-                const C top = EXACT ? c : (C)(c & msk);
-                const uint32_t cls = (uint32_t)(top >= pre) + (uint32_t)(top > pre);
-                const uint32_t reg = (uint32_t)((uint32_t)j >= r1) + (uint32_t)((uint32_t)j >= r2);
-                if (a.op == SOP_ARG && (EXACT || reg != 1)) a.out_idx[p0 + j] = p0 + j;
-                if (!EXACT && cls == 1) {
-                    candm |= 1u << j;
-                    ++ncand;
-                    atomicAdd(&sh[uint32_t(c >> lo) & (uint32_t)(nb - 1)], 1u);
-                }
-                if (cls != reg) {
-                    const uint32_t X = (!EXACT && cls == 1) ? 3u : cls;
-                    const uint32_t R = (!EXACT && reg == 1) ? 3u : reg;
+        for (int q = 0; q < S; ++q) {
+            const size_t p0 = s0 + (size_t)q * WCH + (size_t)lane * IPT;
+            tags[q] = 0xFFFFFFFFu;
+            if (p0 >= n) continue;
+            C raw[IPT];
+            sel_load_chunk<C>(keys, n, p0, vec, raw);
+            const uint32_t r1 = (uint32_t)(b_lo > p0 ? min(b_lo - p0, (size_t)IPT) : 0);
+            const uint32_t r2 = (uint32_t)(b_hi > p0 ? min(b_hi - p0, (size_t)IPT) : 0);
+            const uint32_t valid = (uint32_t)min(n - p0, (size_t)IPT);
+            uint32_t t4 = 0;
+#pragma unroll
+            for (int j = 0; j < IPT; ++j) {
+                uint32_t t = 0xF;
+                if ((uint32_t)j < valid) {
+                    const C c = cx.to(raw[j]);
+                    const C top = EXACT ? c : (C)(c & msk);
+                    const uint32_t cls = (uint32_t)(top >= pre) + (uint32_t)(top > pre);
+                    const uint32_t reg = (uint32_t)((uint32_t)j >= r1) + (uint32_t)((uint32_t)j >= r2);
+                    if (a.op == SOP_ARG && (EXACT || reg != 1)) a.out_idx[p0 + j] = p0 + j;
+                    uint32_t X = 3u, R = 3u;
+                    if (!EXACT && cls == 1) {
+                        X = 1u;                  // candidate
+                        ++ncand;
+                        atomicAdd(&sh[uint32_t(c >> lo) & (uint32_t)(nb - 1)], 1u);
+                    }
+                    if (cls != reg) {
+                        if (EXACT && !(keys_only_exact && cls == 1)) X = cls;
+                        else if (!EXACT && cls != 1) X = cls;
+                        if (EXACT || reg != 1) R = reg;
+                    }
+                    if (X != 3u && !(!EXACT && X == 1u)) lists += 1ull << (16 * X);
+                    if (R != 3u) holes += 1ull << (16 * R);
                     t = X | (R << 2);
-                    if (X != 3u) lists += 1u << (10 * X);
-                    if (R != 3u) holes += 1u << (10 * R);
                 }
+                t4 |= t << (4 * j);
             }
-            tags |= t << (4 * j);
+            tags[q] = t4;
         }
-        if (!__any_sync(0xffffffffu, (lists | holes | ncand) != 0u)) continue;
+        if (!__any_sync(0xffffffffu, (lists | holes | ncand) != 0ull)) continue;
         // warp-inclusive scans of the packed counts
-        uint32_t il = lists, ih = holes, ic = ncand;
+        unsigned long long il = lists, ih = holes;
+        uint32_t ic = ncand;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
-            const uint32_t yl = __shfl_up_sync(0xffffffffu, il, o);
-            const uint32_t yh = __shfl_up_sync(0xffffffffu, ih, o);
+            const unsigned long long yl = __shfl_up_sync(0xffffffffu, il, o);
+            const unsigned long long yh = __shfl_up_sync(0xffffffffu, ih, o);
             const uint32_t yc = __shfl_up_sync(0xffffffffu, ic, o);
             if (lane >= o) {
                 il += yl;
@@ -341,14 +358,14 @@ __global__ void __launch_bounds__(256) sel_split_kernel(SelArgs a, int lo, int b
             }
         }
         // lane 31 holds the warp's totals: reserve slots, one atomic per list
-        size_t base = 0;
-        const uint32_t tl = __shfl_sync(0xffffffffu, il, 31);
-        const uint32_t th = __shfl_sync(0xffffffffu, ih, 31);
+        const unsigned long long tl = __shfl_sync(0xffffffffu, il, 31);
+        const unsigned long long th = __shfl_sync(0xffffffffu, ih, 31);
         const uint32_t tc = __shfl_sync(0xffffffffu, ic, 31);
+        size_t base = 0;
         if (lane < 7) {
             uint32_t t = 0;
-            if (lane < 3) t = (tl >> (10 * lane)) & 0x3FFu;
-            else if (lane < 6) t = (th >> (10 * (lane - 3))) & 0x3FFu;
+            if (lane < 3) t = (uint32_t)(tl >> (16 * lane)) & 0xFFFFu;
+            else if (lane < 6) t = (uint32_t)(th >> (16 * (lane - 3))) & 0xFFFFu;
             else t = tc;
             if (t) {
                 const int q = lane < 3 ? lane : lane - 3;
@@ -357,7 +374,7 @@ __global__ void __launch_bounds__(256) sel_split_kernel(SelArgs a, int lo, int b
                 else if (lane < 6) base = rs + atomicAdd(&a.st->nhole[q], t);
                 else base = (size_t)atomicAdd(&a.st->cand_n, (unsigned long long)t);
                 // a list that would run past its space (never, with consistent
-                // counts) is not written for this chunk
+                // counts) is not written for this super-chunk
                 if (base + t > n) base = ~size_t(0);
             }
         }
@@ -367,47 +384,62 @@ __global__ void __launch_bounds__(256) sel_split_kernel(SelArgs a, int lo, int b
         for (int q = 0; q < 7; ++q) {
             const size_t b0 = __shfl_sync(0xffffffffu, base, q);
             ok[q] = b0 != ~size_t(0);
-            const uint32_t excl = q < 3 ? ((il - lists) >> (10 * q)) & 0x3FFu
-                                : q < 6 ? ((ih - holes) >> (10 * (q - 3))) & 0x3FFu
+            const uint32_t excl = q < 3 ? (uint32_t)((il - lists) >> (16 * q)) & 0xFFFFu
+                                : q < 6 ? (uint32_t)((ih - holes) >> (16 * (q - 3))) & 0xFFFFu
                                         : ic - ncand;
             slot[q] = b0 + excl;
         }
+#pragma unroll 1
+        for (int q = 0; q < S; ++q) {
+            const uint32_t t4 = tags[q];
+            // 0xF per element: nothing to record
+            bool any = false;
 #pragma unroll
-        for (int j = 0; j < IPT; ++j) {
-            const size_t p = p0 + j;
-            const uint32_t X = (tags >> (4 * j)) & 3u, R = (tags >> (4 * j + 2)) & 3u;
+            for (int j = 0; j < IPT; ++j) any |= ((t4 >> (4 * j)) & 0xFu) != 0xFu;
+            if (!any) continue;
+            const size_t p0 = s0 + (size_t)q * WCH + (size_t)lane * IPT;
+            C raw[IPT];
+            sel_load_chunk<C>(keys, n, p0, vec, raw);
 #pragma unroll
-            for (int q = 0; q < 3; ++q) {
-                if (!EXACT && q == 1) continue;
-                if (X == (uint32_t)q) {
-                    if (ok[q]) {
-                        const size_t at = slot[q];
+            for (int j = 0; j < IPT; ++j) {
+                const size_t p = p0 + j;
+                const uint32_t X = (t4 >> (4 * j)) & 3u, R = (t4 >> (4 * j + 2)) & 3u;
+                if (!EXACT && X == 1u) {           // candidate
+                    if (ok[6]) {
+                        const size_t at = slot[6];
+                        cand[at] = cx.to(raw[j]);
                         if (a.op == SOP_ARG) {
-                            reinterpret_cast<uint32_t *>(a.mis_v)[at] = (uint32_t)p;
-                        } else {
-                            mis_k[at] = raw[j];
-                            if constexpr (HAS_V)
-                                if (a.op == SOP_KV) mis_v[at] = vals[p];
+                            static_cast<uint32_t *>(a.cand_p)[at] = (uint32_t)p;
+                        } else if constexpr (HAS_V) {
+                            if (a.op == SOP_KV) static_cast<V *>(a.cand_p)[at] = vals[p];
                         }
                     }
-                    ++slot[q];
-                }
-                if (R == (uint32_t)q) {
-                    if (ok[3 + q]) a.holes[slot[3 + q]] = (uint32_t)p;
-                    ++slot[3 + q];
-                }
-            }
-            if (!EXACT && ((candm >> j) & 1u)) {
-                if (ok[6]) {
-                    const size_t at = slot[6];
-                    cand[at] = cx.to(raw[j]);
-                    if (a.op == SOP_ARG) {
-                        static_cast<uint32_t *>(a.cand_p)[at] = (uint32_t)p;
-                    } else if constexpr (HAS_V) {
-                        if (a.op == SOP_KV) static_cast<V *>(a.cand_p)[at] = vals[p];
+                    ++slot[6];
+                } else if (X != 3u) {
+#pragma unroll
+                    for (int x = 0; x < 3; ++x) {
+                        if (X != (uint32_t)x) continue;
+                        if (ok[x]) {
+                            const size_t at = slot[x];
+                            if (a.op == SOP_ARG) {
+                                reinterpret_cast<uint32_t *>(a.mis_v)[at] = (uint32_t)p;
+                            } else {
+                                mis_k[at] = raw[j];
+                                if constexpr (HAS_V)
+                                    if (a.op == SOP_KV) mis_v[at] = vals[p];
+                            }
+                        }
+                        ++slot[x];
                     }
                 }
-                ++slot[6];
+                if (R != 3u) {
+#pragma unroll
+                    for (int r = 0; r < 3; ++r) {
+                        if (R != (uint32_t)r) continue;
+                        if (ok[3 + r]) a.holes[slot[3 + r]] = (uint32_t)p;
+                        ++slot[3 + r];
+                    }
+                }
             }
         }
     }
@@ -502,6 +534,10 @@ __global__ void __launch_bounds__(256) sel_place_kernel(SelArgs a, int exact)
     const C *mis_k = static_cast<const C *>(a.mis_k);
     const V *mis_v = static_cast<const V *>(a.mis_v);
     const size_t stride = (size_t)gridDim.x * 256;
+    // keys-only exact partitions list no element equal to K: its region's
+    // holes get K itself
+    const C kval = from_code((C)a.st->prefix, a.xf);
+    const bool fill_k = exact && a.op == SOP_KEYS;
     for (int X = 0; X < 3; X += exact ? 1 : 2) {
         const size_t rs = X == 0 ? 0 : (X == 1 ? a.st->b_lo : b_hi);
         // counts are consistent by construction; clamp so a broken state can
@@ -516,7 +552,8 @@ __global__ void __launch_bounds__(256) sel_place_kernel(SelArgs a, int exact)
             for (int u = 0; u < U; ++u) {
                 const size_t j = j0 + u * stride;
                 pos[u] = j < cnt ? a.holes[rs + j] : 0xffffffffu;
-                mk[u] = (j < cnt && a.op != SOP_ARG) ? mis_k[rs + j] : C(0);
+                mk[u] = (j < cnt && a.op != SOP_ARG) ? (X == 1 && fill_k ? kval : mis_k[rs + j])
+                                                      : C(0);
             }
 #pragma unroll
             for (int u = 0; u < U; ++u) {
