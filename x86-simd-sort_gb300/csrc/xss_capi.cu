@@ -189,6 +189,13 @@ static int gpu_partial_qsort(int dt, void *d, size_t k, size_t n, int hasnan, in
     KeyXform sort_xf{di.kind, desc ? 1 : 0, hasnan ? 1 : 0};
     if (n <= SMALL_SORT_MAX || k == n)
         return gpu_qsort(dt, d, (k == n) ? n : n, hasnan, desc, ws, wsb, s);
+    if (count16_wanted(SOP_KEYS, di.kbytes, n)) {
+        // 16-bit keys: one full sort by counting; canonical NaNs only in the
+        // sorted prefix, as select + prefix sort would leave them
+        rc = resolve_ws(s, count16_workspace_bytes(n), ws, wsb);
+        if (rc) return rc;
+        return count16_sort(sort_xf, d, n, k, ws, wsb, s);
+    }
     KeyXform sel_xf{di.kind, desc ? 1 : 0, 0};
     const size_t need = std::max(select_workspace_bytes(SOP_KEYS, di.kbytes, 0, n),
                                  radix_workspace_bytes(SOP_KEYS, di.kbytes, 0, k));

@@ -97,6 +97,20 @@ bool host_pipeline_wanted(size_t n);
 int host_pipelined_sort(int op, int kbytes, KeyXform xf, void *hk, void *hv, int vbytes,
                         uint64_t *hidx, size_t n);
 
+// Keys-only sorts of 16-bit keys above COUNT16_MIN_N keys count every code
+// instead of radix sorting (xss_count16.cu); radix_sort, radix_select and
+// their workspace sizes route there.  canon_end: sorted positions below it
+// get canonical NaNs when xf.canon is set.
+constexpr size_t COUNT16_MIN_N = size_t(1) << 15;
+bool count16_wanted(int op, int kbytes, size_t n);
+size_t count16_workspace_bytes(size_t n);
+int count16_sort(KeyXform xf, void *keys, size_t n, size_t canon_end, void *ws, size_t ws_bytes,
+                 cudaStream_t s);
+
+// Workspace of radix_sort_chunk (a radix sort of at most XSS_RADIX_MAX_N keys,
+// never the counting form).
+size_t radix_chunk_workspace_bytes(int op, int kbytes, int vbytes, size_t n);
+
 size_t select_workspace_bytes(int op, int kbytes, int vbytes, size_t n);
 // Partition so that position k holds the k-th element in code order,
 // smaller codes before it and larger after.  keys are modified in place for

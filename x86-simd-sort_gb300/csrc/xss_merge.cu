@@ -174,7 +174,7 @@ static BigLayout big_layout(int op, int kbytes, int vbytes, size_t n)
     const int vb = op == SOP_ARG ? 8 : (op == SOP_KV ? vbytes : 0);
     size_t off = 0;
     L.chunk_ws = off;
-    off = align_up(off + radix_workspace_bytes(sop, kbytes, vb, merge_chunk()), 256);
+    off = align_up(off + radix_chunk_workspace_bytes(sop, kbytes, vb, merge_chunk()), 256);
     L.k0 = off;
     if (op == SOP_ARG) off = align_up(off + n * kbytes, 256);
     L.k1 = off;
@@ -266,7 +266,7 @@ static int big_sort_c(int op, KeyXform xf, void *keys, void *vals, int vbytes,
                       cudaStream_t s)
 {
     const int kb = sizeof(C);
-    const size_t cws_bytes = radix_workspace_bytes(op == SOP_ARG ? SOP_KV : op, kb,
+    const size_t cws_bytes = radix_chunk_workspace_bytes(op == SOP_ARG ? SOP_KV : op, kb,
                                                    op == SOP_ARG ? 8 : vbytes, merge_chunk());
     void *cws = ws + L.chunk_ws;
     size_t *split = reinterpret_cast<size_t *>(ws + L.split);
@@ -412,7 +412,7 @@ static int pipelined_sort_c(int op, KeyXform xf, C *hk, V *hv, uint64_t *hidx, s
     if (nch > 64) return XSS_ETOOBIG;
     // device layout: keys, values, one chunk's radix workspace, the merge's
     // partner buffers and split points
-    const size_t cws_bytes = radix_workspace_bytes(sop, kb, (int)VB, chunk);
+    const size_t cws_bytes = radix_chunk_workspace_bytes(sop, kb, (int)VB, chunk);
     size_t off = 0;
     const size_t o_k = off;  off = align_up(off + n * kb, 256);
     const size_t o_v = off;  off = align_up(off + n * VB, 256);

@@ -139,7 +139,7 @@ const char *xss_prof_kind_name(int kind)
     static const char *names[PK_COUNT] = {"hist", "onesweep", "fixup", "small_sort",
                                           "sel_hist", "sel_find", "sel_collect", "sel_place",
                                           "seg_small", "seg_block", "seg_misc", "object",
-                                          "merge"};
+                                          "merge", "count16"};
     return (kind >= 0 && kind < PK_COUNT) ? names[kind] : "unknown";
 }
 

@@ -18,7 +18,8 @@ enum ProfKind : int {
     PK_SEG_MISC = 10,  // segmented sort: binning / bookkeeping
     PK_OBJECT = 11,    // record sort: key extraction / record gather
     PK_MERGE = 12,     // chunked sort of a very large array: merge of sorted runs
-    PK_COUNT = 13
+    PK_COUNT16 = 13,   // 16-bit keys-only sort by counting: counts, scan, expansion
+    PK_COUNT = 14
 };
 
 void prof_begin(cudaStream_t s, int kind);

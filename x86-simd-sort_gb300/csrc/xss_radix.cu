@@ -354,11 +354,18 @@ static size_t tile_for_bytes(int op, int kbytes, int vbytes, size_t n)
     }
 }
 
+size_t radix_chunk_workspace_bytes(int op, int kbytes, int vbytes, size_t n)
+{
+    if (n <= SMALL_SORT_MAX) return 0;
+    return radix_layout(op, kbytes, vbytes, n, tile_for_bytes(op, kbytes, vbytes, n)).total;
+}
+
 size_t radix_workspace_bytes(int op, int kbytes, int vbytes, size_t n)
 {
     if (n <= SMALL_SORT_MAX) return 0;
+    if (count16_wanted(op, kbytes, n)) return count16_workspace_bytes(n);
     if (big_sort_needed(n)) return big_sort_workspace_bytes(op, kbytes, vbytes, n);
-    return radix_layout(op, kbytes, vbytes, n, tile_for_bytes(op, kbytes, vbytes, n)).total;
+    return radix_chunk_workspace_bytes(op, kbytes, vbytes, n);
 }
 
 // How a sort is launched: where device-side errors go and whether launches
@@ -601,6 +608,7 @@ int radix_sort(int op, int kbytes, KeyXform xf, void *keys, void *vals, int vbyt
                uint64_t *out_idx, size_t n, void *ws, size_t ws_bytes, cudaStream_t s)
 {
     if (n > XSS_MAX_N) return XSS_ETOOBIG;
+    if (count16_wanted(op, kbytes, n)) return count16_sort(xf, keys, n, n, ws, ws_bytes, s);
     if (big_sort_needed(n))
         return big_sort(op, kbytes, xf, keys, vals, vbytes, out_idx, n, ws, ws_bytes, s);
     return radix_sort_chunk(op, kbytes, xf, keys, vals, vbytes, out_idx, n, ws, ws_bytes, s);
@@ -660,7 +668,7 @@ static int noalloc_prepare(unsigned char *scratch, cudaStream_t s)
     XSS_CUDA_TRY(cudaMemsetAsync(scratch, 0, NOALLOC_ERR_BYTES, s));
     for (int kbytes : {2, 4, 8}) {
         for (size_t n : {size_t(64), SMALL_SORT_MAX + 904}) {
-            const size_t wsb = align_up(radix_workspace_bytes(SOP_KEYS, kbytes, 0, n), 256);
+            const size_t wsb = align_up(radix_chunk_workspace_bytes(SOP_KEYS, kbytes, 0, n), 256);
             unsigned char *ws = scratch + NOALLOC_ERR_BYTES;
             unsigned char *keys = ws + wsb;
             if (wsb + n * kbytes > NOALLOC_WS_BYTES) return XSS_ENOMEM;

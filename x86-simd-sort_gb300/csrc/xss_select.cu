@@ -594,6 +594,7 @@ static SelLayout sel_layout(int op, int kbytes, int vbytes, size_t n)
 size_t select_workspace_bytes(int op, int kbytes, int vbytes, size_t n)
 {
     if (n <= SMALL_SORT_MAX) return 0;
+    if (count16_wanted(op, kbytes, n)) return count16_workspace_bytes(n);
     // beyond one radix sort's size the select is a full (chunked) sort
     if (big_sort_needed(n)) return radix_workspace_bytes(op, kbytes, vbytes, n);
     return sel_layout(op, kbytes, vbytes, n).total;
@@ -695,6 +696,9 @@ int radix_select(int op, int kbytes, KeyXform xf, void *keys, void *vals, int vb
         // beyond one radix sort's size, which the chunked sort takes)
         return radix_sort(op, kbytes, xf, keys, vals, vbytes, out_idx, n, ws, ws_bytes, s);
     }
+    // 16-bit keys only: a full sort by counting (two memory passes) satisfies
+    // the select contract and costs less than the partition
+    if (count16_wanted(op, kbytes, n)) return count16_sort(xf, keys, n, 0, ws, ws_bytes, s);
     switch (kbytes) {
     case 2: return select_c<uint16_t>(op, xf, keys, vals, vbytes, out_idx, k, n, ws, ws_bytes, s);
     case 4: return select_c<uint32_t>(op, xf, keys, vals, vbytes, out_idx, k, n, ws, ws_bytes, s);

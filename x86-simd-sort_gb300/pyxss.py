@@ -85,7 +85,7 @@ _SIGS = {
 
 PROF_KINDS = ["hist", "onesweep", "fixup", "small_sort", "sel_hist", "sel_find",
               "sel_collect", "sel_place", "seg_small", "seg_block", "seg_misc", "object",
-              "merge"]
+              "merge", "count16"]
 
 
 def prof_enable(on: bool) -> None:
