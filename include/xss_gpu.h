@@ -92,6 +92,16 @@ int xss_gpu_stream_status(xss_stream_t stream);
  */
 int xss_gpu_selftest_bounded_wait(int which, unsigned spin_limit, xss_stream_t stream);
 
+/*
+ * Self test of the hardware property the radix pass's ranking relies on (no
+ * counterpart in the reference): shared-memory atomic adds that lanes of one
+ * warp instruction make to one address return their results in lane order.
+ * Runs about 300 million such adds of many collision patterns on the current
+ * device and stores the number that broke lane order in *violations (0 on
+ * every GB300 measured).  Synchronous.
+ */
+int xss_gpu_selftest_rank_order(unsigned long long *violations, xss_stream_t stream);
+
 /* ------------------------------------------------------------------ */
 /* Device-pointer entry points.  Arrays live in device memory; work is   */
 /* enqueued on `stream` and the call returns without synchronising      */

@@ -40,3 +40,17 @@ def test_bounded_wait_times_out_and_context_survives(xss, cuda, which):
     y = x.copy()
     xss.qsort(y)
     assert_same_sorted(y, ref_sorted(x), "sort after a timed-out wait")
+
+
+def test_rank_order_of_shared_atomics(xss, cuda):
+    """The radix pass ranks each key by the result of its shared-memory count
+    atomic; that is stable only if same-address atomics of one warp
+    instruction return in lane order.  The library's self test checks it on
+    this device over about 300 million collisions of many patterns."""
+    import ctypes
+    f = xss.lib().xss_gpu_selftest_rank_order
+    f.restype = ctypes.c_int
+    f.argtypes = [ctypes.POINTER(ctypes.c_ulonglong), ctypes.c_void_p]
+    v = ctypes.c_ulonglong(123)
+    assert f(ctypes.byref(v), None) == 0
+    assert v.value == 0

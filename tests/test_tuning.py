@@ -28,7 +28,7 @@ def test_candidate_lines_are_well_formed():
             block, items, minb, lb, rank, persist, dpt = f
             assert block % 32 == 0 and 256 <= block <= 1024
             assert items >= 1 and minb >= 1 and lb in (8, 16, 32)
-            assert rank in (0, 1) and persist in (0, 1, 2) and dpt in (0, 1, 2, 4)
+            assert rank in (0, 1, 2) and persist in (0, 1, 2) and dpt in (0, 1, 2, 4)
 
 
 def test_committed_header_covers_every_class():
@@ -38,12 +38,12 @@ def test_committed_header_covers_every_class():
         for macro in ("XSS_CFG_" + cls, "XSS_CFGM_" + cls):
             assert macro in lines, macro
             f = [int(x) for x in lines[macro].split(",")]
-            assert len(f) == 7 and f[0] % 32 == 0 and f[4] in (0, 1)
+            assert len(f) == 7 and f[0] % 32 == 0 and f[4] in (0, 1, 2)
 
 
 def test_a_candidate_line_builds_into_its_own_library():
     """The tuner's variant build (one pre-included line, the radix unit
     recompiled, linked with the shared objects) works without a GPU."""
     common = autotune.build_common()
-    so = autotune.build_variant("K32", "320,20,3,8,0,1,0", common)
+    so = autotune.build_variant("K32", "320,20,3,8,2,1,0", common)
     assert os.path.exists(so) and os.path.getsize(so) > 0

@@ -47,19 +47,21 @@ CLASSES = {
 # Candidate lines (BLOCK, ITEMS, MINB, LB, RANK, PERSIST, DPT).  They stay
 # within 64K registers per SM at MINB CTAs and the 227 KB shared-memory cap.
 CANDIDATES = {
-    "K16": ["320,20,3,16,0,1,0", "256,24,3,16,0,1,0", "512,16,2,16,0,1,0"],
-    "K32": ["320,20,3,16,0,1,0", "256,24,3,16,0,1,0", "512,16,2,16,0,1,0", "320,24,2,16,0,1,0"],
-    "K64": ["512,16,1,16,0,1,1", "512,12,1,16,0,1,1", "256,16,2,16,0,1,0"],
-    "K32V32": ["512,12,1,16,0,1,1", "512,10,2,16,0,0,1", "512,14,1,16,0,1,1"],
-    "K64V64": ["512,11,1,16,1,1,1", "512,11,1,16,0,1,1", "512,10,1,16,0,1,1", "512,12,1,16,0,1,1"],
-    "DEFAULT": ["512,14,1,16,0,1,1", "512,12,1,16,0,1,1", "512,14,1,16,1,1,1"],
+    "K16": ["320,20,3,16,2,1,0", "512,16,2,16,2,1,0"],
+    "K32": ["320,20,3,8,2,1,0", "320,20,3,16,2,1,0", "512,16,2,8,2,1,0", "384,16,3,8,2,1,0",
+            "256,24,3,8,2,1,0", "256,16,4,8,2,1,0", "320,16,4,8,2,1,0"],
+    "K64": ["512,16,1,16,2,1,1", "512,20,1,16,2,1,1", "512,24,1,16,2,1,1", "768,16,1,16,2,1,1"],
+    "K32V32": ["512,14,1,16,2,1,1", "512,20,1,16,2,1,1", "768,14,1,16,2,1,1"],
+    "K64V64": ["512,11,1,8,2,1,1", "512,12,1,8,2,1,1", "640,10,1,8,2,1,1", "768,8,1,8,2,1,1",
+               "384,16,1,8,2,1,1", "512,12,1,16,2,1,1"],
+    "DEFAULT": ["512,14,1,8,2,1,1", "512,16,1,8,2,1,1", "640,12,1,8,2,1,1", "768,10,1,8,2,1,1"],
     # mid-size arrays: several CTAs per SM (tile or resident form)
-    "K16_MID": ["512,16,2,16,0,1,0", "256,16,3,16,0,1,0"],
-    "K32_MID": ["512,16,2,16,0,1,0", "256,16,3,16,0,1,0", "512,8,2,16,0,0,1"],
-    "K64_MID": ["512,8,2,16,0,1,1", "256,16,2,16,1,1,0", "256,16,2,16,0,1,0"],
-    "K32V32_MID": ["512,10,2,16,1,0,0", "512,10,2,16,0,0,0", "512,6,2,16,1,0,1"],
-    "K64V64_MID": ["512,6,2,16,1,0,1", "512,6,2,16,0,0,1", "256,12,2,16,1,0,0"],
-    "DEFAULT_MID": ["512,6,2,16,0,0,1", "256,12,2,16,1,0,0", "256,8,3,16,1,0,0"],
+    "K16_MID": ["512,16,2,16,2,1,0", "256,16,3,16,2,1,0"],
+    "K32_MID": ["512,16,2,16,2,1,0", "256,16,3,16,2,1,0", "256,8,4,16,2,1,0"],
+    "K64_MID": ["512,8,2,16,2,1,1", "256,16,2,16,2,1,0"],
+    "K32V32_MID": ["512,10,2,16,2,0,0", "512,10,2,16,2,1,1"],
+    "K64V64_MID": ["512,6,2,16,2,0,1", "256,12,2,16,2,0,0"],
+    "DEFAULT_MID": ["512,6,2,16,2,0,1", "256,8,3,16,2,0,0"],
 }
 
 

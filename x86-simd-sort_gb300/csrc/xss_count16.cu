@@ -103,31 +103,26 @@ __global__ void __launch_bounds__(C16_HIST_BLOCK, 1) c16_hist_kernel(C16Args a)
     for (int i = tid; i < C16_WORDS / 4; i += C16_HIST_BLOCK) dst[i] = s4[i];
 }
 
-// Total count of every code: the CTAs' counters plus the overflow (written
-// into `over`, which then holds the totals).
-__global__ void __launch_bounds__(256) c16_reduce_kernel(C16Args a, int parts)
+// Total of every code (the CTAs' counters plus the overflow) and its first
+// position within its block of 1024 codes; one CTA per block, one counter
+// word (two codes) per thread.  The block totals go to bsum.
+constexpr int C16_SCAN_BLOCK = 256;                        // words per block
+constexpr int C16_SCAN_CODES = 2 * C16_SCAN_BLOCK;         // codes per block
+constexpr int C16_NBLK = C16_BINS / C16_SCAN_CODES;        // 128
+__global__ void __launch_bounds__(C16_SCAN_BLOCK) c16_reduce_kernel(C16Args a, int parts,
+                                                                     unsigned long long *bsum)
 {
-    const int w = blockIdx.x * 256 + threadIdx.x;
-    if (w >= C16_WORDS) return;
-    unsigned long long lo = 0, hi = 0;
+    __shared__ unsigned long long s_warp[C16_SCAN_BLOCK / 32];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int w = blockIdx.x * C16_SCAN_BLOCK + tid;
+    unsigned long long lo = a.over[2 * w], hi = a.over[2 * w + 1];
+#pragma unroll 8
     for (int c = 0; c < parts; ++c) {
         const uint32_t v = a.part[(size_t)c * C16_WORDS + w];
         lo += v & 0xFFFFu;
         hi += v >> 16;
     }
-    a.over[2 * w] += lo;
-    a.over[2 * w + 1] += hi;
-}
-
-// Exclusive scan of the totals into the first position of every code (one
-// CTA, 64 codes per thread).
-__global__ void __launch_bounds__(1024) c16_scan_kernel(C16Args a)
-{
-    constexpr int PER = C16_BINS / 1024;
-    __shared__ unsigned long long s_warp[32];
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    unsigned long long sum = 0;
-    for (int i = 0; i < PER; ++i) sum += a.over[tid * PER + i];
+    const unsigned long long sum = lo + hi;
     unsigned long long x = sum;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
@@ -137,71 +132,132 @@ __global__ void __launch_bounds__(1024) c16_scan_kernel(C16Args a)
     if (lane == 31) s_warp[warp] = x;
     __syncthreads();
     if (warp == 0) {
-        unsigned long long t = s_warp[lane];
+        unsigned long long t = lane < C16_SCAN_BLOCK / 32 ? s_warp[lane] : 0ull;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
             const unsigned long long y = __shfl_up_sync(0xffffffffu, t, o);
             if (lane >= o) t += y;
         }
-        s_warp[lane] = t;
+        if (lane < C16_SCAN_BLOCK / 32) s_warp[lane] = t;
     }
     __syncthreads();
-    unsigned long long run = (warp ? s_warp[warp - 1] : 0ull) + x - sum;
-    for (int i = 0; i < PER; ++i) {
-        a.start[tid * PER + i] = run;
-        run += a.over[tid * PER + i];
+    const unsigned long long ex = (warp ? s_warp[warp - 1] : 0ull) + x - sum;
+    a.start[2 * w] = ex;
+    a.start[2 * w + 1] = ex + lo;
+    if (tid == C16_SCAN_BLOCK - 1) bsum[blockIdx.x] = ex + sum;
+}
+
+// Add every block's offset (exclusive scan of the 128 block totals); start[BINS] = n.
+__global__ void __launch_bounds__(1024) c16_offsets_kernel(C16Args a,
+                                                           const unsigned long long *bsum)
+{
+    __shared__ unsigned long long s_off[C16_NBLK];
+    const int tid = threadIdx.x, lane = tid & 31;
+    constexpr int PER = C16_NBLK / 32;   // blocks per lane
+    static_assert(C16_NBLK % 32 == 0, "whole blocks per lane");
+    if (tid < 32) {
+        unsigned long long b[PER], x = 0;
+#pragma unroll
+        for (int i = 0; i < PER; ++i) {
+            b[i] = bsum[PER * lane + i];
+            x += b[i];
+        }
+        const unsigned long long tot = x;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const unsigned long long y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
+        }
+        unsigned long long ex = x - tot;
+#pragma unroll
+        for (int i = 0; i < PER; ++i) {
+            s_off[PER * lane + i] = ex;
+            ex += b[i];
+        }
     }
+    __syncthreads();
+    for (int i = tid; i < C16_BINS; i += 1024) a.start[i] += s_off[i / C16_SCAN_CODES];
     if (tid == 0) a.start[C16_BINS] = a.n;
 }
 
 // The code at sorted position p (0 <= p < n): the last code whose first
-// position is <= p.  Two levels: the block's shared copy of every 32nd
-// code's first position picks the block of 32 codes, then five probes of
-// start[] (L1/L2) pick the code in it.
-constexpr int C16_COARSE = 32;                               // codes per coarse entry
-constexpr int C16_NCOARSE = C16_BINS / C16_COARSE;           // 2048
-__device__ __forceinline__ uint32_t c16_code_at(const unsigned long long *s_coarse,
-                                                const unsigned long long *start, size_t p)
+// position is <= p, by binary search of start[lo .. hi] (start[lo] <= p,
+// and p < start[hi + 1]).
+__device__ __forceinline__ uint32_t c16_search(const unsigned long long *start, size_t p,
+                                               uint32_t lo, uint32_t hi)
 {
-    uint32_t lo = 0, hi = C16_NCOARSE - 1;   // s_coarse[0] = 0 <= p
     while (lo < hi) {
         const uint32_t mid = (lo + hi + 1) >> 1;
-        if (s_coarse[mid] <= p) lo = mid;
+        if (start[mid] <= p) lo = mid;
         else hi = mid - 1;
     }
-    uint32_t c = lo * C16_COARSE;
-    uint32_t top = c + C16_COARSE - 1;
-    while (c < top) {
-        const uint32_t mid = (c + top + 1) >> 1;
-        if (start[mid] <= p) c = mid;
-        else top = mid - 1;
-    }
-    return c;
+    return lo;
 }
 
-// Write the sorted keys: each thread 8 consecutive positions (one 16-byte
-// store where aligned), stepping to the next code inside its eight positions
-// when it crosses a code's end.
-__global__ void __launch_bounds__(C16_EXPAND_BLOCK) c16_expand_kernel(C16Args a)
+// Output chunks: C16_CHUNK positions from the first 16-byte boundary on
+// (positions before it, fewer than eight, belong to chunk 0's first CTA).
+constexpr int C16_EXPAND_ITERS = 4;                                      // 16-byte stores per thread
+constexpr size_t C16_CHUNK = (size_t)C16_EXPAND_BLOCK * C16_GROUP * C16_EXPAND_ITERS;  // 8192
+constexpr int C16_RANGE_MAX = 2047;   // codes per chunk held in shared memory
+
+// first[q] = the code at the chunk's first position (q < chunks), and
+// first[chunks] = the code at position n - 1; one search per thread.
+__global__ void __launch_bounds__(256) c16_chunk_kernel(C16Args a, uint32_t *first,
+                                                        size_t chunks, size_t head)
 {
-    __shared__ unsigned long long s_coarse[C16_NCOARSE];
-    for (int i = threadIdx.x; i < C16_NCOARSE; i += C16_EXPAND_BLOCK)
-        s_coarse[i] = a.start[(size_t)i * C16_COARSE];
-    __syncthreads();
+    const size_t q = (size_t)blockIdx.x * 256 + threadIdx.x;
+    if (q > chunks) return;
+    const size_t p = q < chunks ? head + q * C16_CHUNK : a.n - 1;
+    first[q] = c16_search(a.start, p, 0, C16_BINS - 1);
+}
+
+// Write the sorted keys, one chunk per CTA: the starts of the chunk's codes
+// come into shared memory (or, for a chunk spanning more codes than fit,
+// are searched in place), then each thread writes 8 consecutive positions
+// per 16-byte store, stepping to the next code where one ends.
+__global__ void __launch_bounds__(C16_EXPAND_BLOCK) c16_expand_kernel(C16Args a,
+                                                                      const uint32_t *first,
+                                                                      size_t chunks, size_t head)
+{
+    __shared__ unsigned long long s_start[C16_RANGE_MAX + 2];
+    const size_t q = blockIdx.x;
     const Codec<uint16_t> cx(a.xf);
-    const unsigned long long *start = a.start;
     uint16_t *dst = a.keys;
     const size_t n = a.n;
-    const size_t head = c16_head(dst, n);
-    // group 0 = the unaligned head; group g >= 1 = [head + 8(g-1), head + 8g)
-    const size_t groups = 1 + (n - head + C16_GROUP - 1) / C16_GROUP;
-    const size_t stride = (size_t)gridDim.x * C16_EXPAND_BLOCK;
-    for (size_t g = (size_t)blockIdx.x * C16_EXPAND_BLOCK + threadIdx.x; g < groups; g += stride) {
-        const size_t p0 = g == 0 ? 0 : head + (g - 1) * C16_GROUP;
-        const size_t p1 = g == 0 ? head : min(n, p0 + C16_GROUP);
-        if (p0 >= p1) continue;
-        uint32_t c = c16_code_at(s_coarse, start, p0);
-        unsigned long long next = start[c + 1];
+    const uint32_t c0 = first[q], c1 = first[q + 1];
+    const bool local = c1 - c0 <= (uint32_t)C16_RANGE_MAX;
+    if (local)
+        for (uint32_t i = threadIdx.x; i <= c1 - c0 + 1; i += C16_EXPAND_BLOCK)
+            s_start[i] = a.start[c0 + i];
+    __syncthreads();
+    auto start_of = [&](uint32_t c) -> unsigned long long {
+        return local ? s_start[c - c0] : a.start[c];
+    };
+    auto code_at = [&](size_t p, uint32_t lo) -> uint32_t {
+        uint32_t hi = c1;
+        while (lo < hi) {
+            const uint32_t mid = (lo + hi + 1) >> 1;
+            if (start_of(mid) <= p) lo = mid;
+            else hi = mid - 1;
+        }
+        return lo;
+    };
+    auto key_at = [&](size_t p, uint32_t c) -> uint16_t {
+        return p < a.canon_end ? cx.from_canon((uint16_t)c) : cx.from((uint16_t)c);
+    };
+    if (q == 0 && threadIdx.x < head) {
+        const size_t p = threadIdx.x;
+        dst[p] = key_at(p, c16_search(a.start, p, 0, c0));
+    }
+    const size_t base = head + q * C16_CHUNK;
+    uint32_t c = c0;
+#pragma unroll 1
+    for (int it = 0; it < C16_EXPAND_ITERS; ++it) {
+        const size_t p0 = base + ((size_t)it * C16_EXPAND_BLOCK + threadIdx.x) * C16_GROUP;
+        if (p0 >= n) break;
+        const size_t p1 = min(n, p0 + C16_GROUP);
+        c = code_at(p0, c);
+        unsigned long long next = start_of(c + 1);
         uint16_t out[C16_GROUP];
 #pragma unroll
         for (int j = 0; j < C16_GROUP; ++j) {
@@ -209,19 +265,19 @@ __global__ void __launch_bounds__(C16_EXPAND_BLOCK) c16_expand_kernel(C16Args a)
             out[j] = 0;
             if (p < p1) {
                 if (p >= next) {
-                    c = c16_code_at(s_coarse, start, p);
-                    next = start[c + 1];
+                    c = code_at(p, c + 1);
+                    next = start_of(c + 1);
                 }
-                out[j] = p < a.canon_end ? cx.from_canon((uint16_t)c) : cx.from((uint16_t)c);
+                out[j] = key_at(p, c);
             }
         }
-        if (p1 - p0 == C16_GROUP && g != 0) {
-            uint4 q;
-            q.x = out[0] | ((uint32_t)out[1] << 16);
-            q.y = out[2] | ((uint32_t)out[3] << 16);
-            q.z = out[4] | ((uint32_t)out[5] << 16);
-            q.w = out[6] | ((uint32_t)out[7] << 16);
-            *reinterpret_cast<uint4 *>(dst + p0) = q;
+        if (p1 - p0 == C16_GROUP) {
+            uint4 v;
+            v.x = out[0] | ((uint32_t)out[1] << 16);
+            v.y = out[2] | ((uint32_t)out[3] << 16);
+            v.z = out[4] | ((uint32_t)out[5] << 16);
+            v.w = out[6] | ((uint32_t)out[7] << 16);
+            *reinterpret_cast<uint4 *>(dst + p0) = v;
         } else {
             for (int j = 0; j < C16_GROUP; ++j)
                 if (p0 + j < p1) dst[p0 + j] = out[j];
@@ -237,8 +293,10 @@ static int c16_grid(size_t n)
 }
 
 struct C16Layout {
-    size_t part, over, start, total;
+    size_t part, over, start, bsum, first, total;
 };
+
+static size_t c16_chunks(size_t n) { return (n + C16_CHUNK - 1) / C16_CHUNK; }
 
 static C16Layout c16_layout(size_t n)
 {
@@ -247,6 +305,8 @@ static C16Layout c16_layout(size_t n)
     L.part = off;  off = align_up(off + (size_t)c16_grid(n) * C16_SMEM, 256);
     L.over = off;  off = align_up(off + sizeof(unsigned long long) * C16_BINS, 256);
     L.start = off; off = align_up(off + sizeof(unsigned long long) * (C16_BINS + 1), 256);
+    L.bsum = off;  off = align_up(off + sizeof(unsigned long long) * C16_NBLK, 256);
+    L.first = off; off = align_up(off + sizeof(uint32_t) * (c16_chunks(n) + 1), 256);
     L.total = off;
     return L;
 }
@@ -279,15 +339,23 @@ int count16_sort(KeyXform xf, void *keys, size_t n, size_t canon_end, void *ws, 
     XSS_CUDA_TRY(cudaMemsetAsync(a.over, 0, sizeof(unsigned long long) * C16_BINS, s));
     XSS_LAUNCH(PK_COUNT16, s, (c16_hist_kernel<<<grid, C16_HIST_BLOCK, C16_SMEM, s>>>(a)));
     XSS_CUDA_TRY(cudaGetLastError());
-    XSS_LAUNCH(PK_COUNT16, s, (c16_reduce_kernel<<<C16_WORDS / 256, 256, 0, s>>>(a, grid)));
+    unsigned long long *bsum = reinterpret_cast<unsigned long long *>(base + L.bsum);
+    uint32_t *first = reinterpret_cast<uint32_t *>(base + L.first);
+    XSS_LAUNCH(PK_COUNT16, s,
+               (c16_reduce_kernel<<<C16_NBLK, C16_SCAN_BLOCK, 0, s>>>(a, grid, bsum)));
     XSS_CUDA_TRY(cudaGetLastError());
-    XSS_LAUNCH(PK_COUNT16, s, (c16_scan_kernel<<<1, 1024, 0, s>>>(a)));
+    XSS_LAUNCH(PK_COUNT16, s, (c16_offsets_kernel<<<1, 1024, 0, s>>>(a, bsum)));
     XSS_CUDA_TRY(cudaGetLastError());
-    const size_t groups = 1 + (n + C16_GROUP - 1) / C16_GROUP;
-    const int eg = (int)std::max<size_t>(
-        1, std::min<size_t>((groups + C16_EXPAND_BLOCK - 1) / C16_EXPAND_BLOCK,
-                            (size_t)num_sms() * 16));
-    XSS_LAUNCH(PK_COUNT16, s, (c16_expand_kernel<<<eg, C16_EXPAND_BLOCK, 0, s>>>(a)));
+    // chunks of the aligned part; the head (< 8 positions) rides with chunk 0
+    const size_t head = std::min(n, (size_t)((16 - (reinterpret_cast<uintptr_t>(keys) & 15)) & 15) / 2);
+    const size_t chunks = std::max<size_t>(1, c16_chunks(n - head));
+    XSS_LAUNCH(PK_COUNT16, s,
+               (c16_chunk_kernel<<<(unsigned)((chunks + 1 + 255) / 256), 256, 0, s>>>(
+                   a, first, chunks, head)));
+    XSS_CUDA_TRY(cudaGetLastError());
+    XSS_LAUNCH(PK_COUNT16, s,
+               (c16_expand_kernel<<<(unsigned)chunks, C16_EXPAND_BLOCK, 0, s>>>(a, first, chunks,
+                                                                               head)));
     XSS_CUDA_TRY(cudaGetLastError());
     return XSS_OK;
 }

@@ -59,7 +59,10 @@ __device__ __forceinline__ void *pick3(void *const (&b)[3], int i)
 //   BLOCK, ITEMS: threads and keys per thread (tile = BLOCK * ITEMS)
 //   MINB:         CTAs per SM the register budget is cut for
 //   LB:           predecessors probed per look-back round trip
-//   RANK:         1 = peer masks from eight ballots, 0 = from shared atomicOr
+//   RANK:         1 = peer masks from eight ballots, 0 = from shared atomicOr,
+//                 2 = the count atomic's return value is the key's rank in its
+//                 warp (shared atomics that meet at one address within a warp
+//                 instruction return in lane order; see rank_order_verified)
 //   PERSIST:      0 = one CTA per tile, 1 = resident CTAs with TMA prefetch,
 //                 2 = resident CTAs with ordinary loads (one staging buffer)
 //   DPT:          look-back placement.  0: after ranking, one digit per
@@ -268,12 +271,23 @@ __device__ __forceinline__ void pass_tile(const RadixArgs &a, const PassDesc &pd
     const uint32_t valid = min((uint32_t)TILE, n - tile_base);
     const uint32_t local0 = (uint32_t)warp * (ITEMS * 32) + lane;
 
-    // ---- digit counts (independent shared atomics): per warp, or per tile
+    // ---- digit counts (independent shared atomics): per warp, or per tile.
+    // RANK 2 keeps each count atomic's result: the number of keys of the same
+    // digit before this one in its warp (program order across items, lane
+    // order within one; the warp barrier orders the items' atomics).
+    constexpr bool KEEP_RANK = RANK == 2;
+    uint32_t wrank[KEEP_RANK ? ITEMS : 1];
     if (tie_free) {
 #pragma unroll
         for (int j = 0; j < ITEMS; ++j)
             if (local0 + j * 32 < valid)
                 atomicAdd(&hist32[uint32_t(key[j] >> shift) & (RADIX - 1)], 1u);
+    } else if constexpr (KEEP_RANK) {
+#pragma unroll
+        for (int j = 0; j < ITEMS; ++j) {
+            wrank[j] = atomicAdd(&wh[uint32_t(key[j] >> shift) & (RADIX - 1)], 1u);
+            __syncwarp();
+        }
     } else {
 #pragma unroll
         for (int j = 0; j < ITEMS; ++j) atomicAdd(&wh[uint32_t(key[j] >> shift) & (RADIX - 1)], 1u);
@@ -348,6 +362,15 @@ __device__ __forceinline__ void pass_tile(const RadixArgs &a, const PassDesc &pd
         for (int j = 0; j < ITEMS; ++j)
             if (local0 + j * 32 < valid)
                 s_k[atomicAdd(&hist32[uint32_t(key[j] >> shift) & (RADIX - 1)], 1u)] = key[j];
+    } else if constexpr (KEEP_RANK) {
+        // staging slot = the warp's start for the digit + the kept rank; the
+        // starts are only read here, so the items are independent
+#pragma unroll
+        for (int j = 0; j < ITEMS; ++j) {
+            const uint32_t p = wh[uint32_t(key[j] >> shift) & (RADIX - 1)] + wrank[j];
+            s_k[p] = key[j];
+            if constexpr (HAS_V) s_v[p] = val[j];
+        }
     } else {
         const uint32_t lt_mask = (1u << lane) - 1u;
         uint32_t *mt = hist32 + (WARPS + warp) * RADIX;   // RANK 0 only
