@@ -258,6 +258,13 @@ __global__ void __launch_bounds__(C16_EXPAND_BLOCK) c16_expand_kernel(C16Args a,
         const size_t p1 = min(n, p0 + C16_GROUP);
         c = code_at(p0, c);
         unsigned long long next = start_of(c + 1);
+        if (p1 - p0 == C16_GROUP && p1 <= next && (p1 <= a.canon_end || p0 >= a.canon_end)) {
+            // the common case: eight copies of one key
+            const uint32_t k = key_at(p0, c);
+            const uint32_t kk = k | (k << 16);
+            *reinterpret_cast<uint4 *>(dst + p0) = make_uint4(kk, kk, kk, kk);
+            continue;
+        }
         uint16_t out[C16_GROUP];
 #pragma unroll
         for (int j = 0; j < C16_GROUP; ++j) {

@@ -94,6 +94,9 @@ int big_sort(int op, int kbytes, KeyXform xf, void *keys, void *vals, int vbytes
 // hidx are host pointers; the call returns once the results are on the host.
 constexpr size_t PIPE_MIN_N = size_t(1) << 22;
 bool host_pipeline_wanted(size_t n);
+// One CPU read per page of a host range, right before a copy reads it
+// (xss_capi.cu explains why).
+void touch_host_pages(const void *p, size_t bytes);
 int host_pipelined_sort(int op, int kbytes, KeyXform xf, void *hk, void *hv, int vbytes,
                         uint64_t *hidx, size_t n);
 

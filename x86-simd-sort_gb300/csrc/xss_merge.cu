@@ -438,11 +438,14 @@ static int pipelined_sort_c(int op, KeyXform xf, C *hk, V *hv, uint64_t *hidx, s
     }
     for (size_t i = 0; i < nch; ++i) {
         const size_t b = i * chunk, len = std::min(chunk, n - b);
+        touch_host_pages(hk + b, len * kb);
         XSS_CUDA_TRY(cudaMemcpyAsync(dk + b, hk + b, len * kb, cudaMemcpyHostToDevice, c->s_in));
         if constexpr (HAS_V)
-            if (op == SOP_KV)
+            if (op == SOP_KV) {
+                touch_host_pages(hv + b, len * VB);
                 XSS_CUDA_TRY(cudaMemcpyAsync(dv + b, hv + b, len * VB, cudaMemcpyHostToDevice,
                                              c->s_in));
+            }
         XSS_CUDA_TRY(cudaEventRecord(c->ev_in[i], c->s_in));
         XSS_CUDA_TRY(cudaStreamWaitEvent(c->s_cmp, c->ev_in[i], 0));
         rc = radix_sort_chunk(sop, kb, xf, dk + b, HAS_V ? (void *)(dv + b) : nullptr, (int)VB,

@@ -67,7 +67,9 @@ __device__ __forceinline__ void *pick3(void *const (&b)[3], int i)
 //                 2 = resident CTAs with ordinary loads (one staging buffer)
 //   DPT:          look-back placement.  0: after ranking, one digit per
 //                 thread; 1, 2, 4: right after the counts, by 256 / DPT
-//                 threads with DPT digits each while the other warps rank
+//                 threads with DPT digits each while the other warps rank;
+//                 12, 14: after ranking, by 128 / 64 threads with 2 / 4
+//                 digits each (fewer walking warps, vector status loads)
 // Each line can be overridden at build time (a pre-included header defining
 // XSS_CFG_K32 etc.) for tuning; xss_tuning.h, written by autotune.py, holds
 // the lines it measured fastest and takes precedence over the defaults below.
@@ -275,8 +277,10 @@ __device__ __forceinline__ void pass_tile(const RadixArgs &a, const PassDesc &pd
     // RANK 2 keeps each count atomic's result: the number of keys of the same
     // digit before this one in its warp (program order across items, lane
     // order within one; the warp barrier orders the items' atomics).
+    // The ranks are below 32 * ITEMS, so two share a register.
     constexpr bool KEEP_RANK = RANK == 2;
-    uint32_t wrank[KEEP_RANK ? ITEMS : 1];
+    static_assert(!KEEP_RANK || 32 * ITEMS < 65536, "ranks fit 16 bits");
+    uint32_t wrank[KEEP_RANK ? (ITEMS + 1) / 2 : 1];
     if (tie_free) {
 #pragma unroll
         for (int j = 0; j < ITEMS; ++j)
@@ -285,7 +289,9 @@ __device__ __forceinline__ void pass_tile(const RadixArgs &a, const PassDesc &pd
     } else if constexpr (KEEP_RANK) {
 #pragma unroll
         for (int j = 0; j < ITEMS; ++j) {
-            wrank[j] = atomicAdd(&wh[uint32_t(key[j] >> shift) & (RADIX - 1)], 1u);
+            const uint32_t r = atomicAdd(&wh[uint32_t(key[j] >> shift) & (RADIX - 1)], 1u);
+            if (j & 1) wrank[j >> 1] |= r << 16;
+            else wrank[j >> 1] = r;
             __syncwarp();
         }
     } else {
@@ -330,8 +336,10 @@ __device__ __forceinline__ void pass_tile(const RadixArgs &a, const PassDesc &pd
     // counts are out, RADIX / DPT threads (the first warps) walk back, DPT
     // digits each, while the other warps already rank; the walkers rank
     // afterwards.  DPT 0: after ranking, one digit per thread.
-    static_assert(DPT == 0 || DPT == 1 || DPT == 2 || DPT == 4, "look-back placement");
-    constexpr int DW = DPT == 0 ? 1 : DPT;   // digits per walking thread
+    static_assert(DPT == 0 || DPT == 1 || DPT == 2 || DPT == 4 || DPT == 12 || DPT == 14,
+                  "look-back placement");
+    constexpr bool LATE = DPT == 0 || DPT >= 10;            // walk after ranking
+    constexpr int DW = DPT == 0 ? 1 : (DPT >= 10 ? (DPT == 12 ? 2 : 4) : DPT);
     auto walk = [&]() {
         const int d0 = tid * DW;
         uint32_t excl[DW];
@@ -348,7 +356,7 @@ __device__ __forceinline__ void pass_tile(const RadixArgs &a, const PassDesc &pd
         for (int j = 0; j < DW; ++j)
             ps.off[d0 + j] = (int32_t)(job.start[d0 + j] + excl[j]) - (int32_t)ps.lstart[d0 + j];
     };
-    if (DPT != 0 && tid < RADIX / DW) walk();
+    if (!LATE && tid < RADIX / DW) walk();
 
     // ---- stable rank (digit, warp, item, lane) and stage in digit order.
     // The lanes sharing a digit find each other either by eight ballots, one
@@ -367,7 +375,8 @@ __device__ __forceinline__ void pass_tile(const RadixArgs &a, const PassDesc &pd
         // starts are only read here, so the items are independent
 #pragma unroll
         for (int j = 0; j < ITEMS; ++j) {
-            const uint32_t p = wh[uint32_t(key[j] >> shift) & (RADIX - 1)] + wrank[j];
+            const uint32_t p = wh[uint32_t(key[j] >> shift) & (RADIX - 1)] +
+                               ((wrank[j >> 1] >> (16 * (j & 1))) & 0xFFFFu);
             s_k[p] = key[j];
             if constexpr (HAS_V) s_v[p] = val[j];
         }
@@ -412,7 +421,7 @@ __device__ __forceinline__ void pass_tile(const RadixArgs &a, const PassDesc &pd
         }
     }
     after_rank();
-    if (DPT == 0 && tid < RADIX) walk();
+    if (LATE && tid < RADIX / DW) walk();
     __syncthreads();
 
     // ---- scatter runs of equal digits to consecutive global addresses

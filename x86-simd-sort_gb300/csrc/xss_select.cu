@@ -450,6 +450,199 @@ __global__ void __launch_bounds__(256) sel_split_kernel(SelArgs a, int lo, int b
     }
 }
 
+// The split pass for 32- and 64-bit keys (B is a bucket of codes sharing
+// the top digit, so its keys become candidates), by warp votes.  Every lane
+// loads SPL_VECS 16-byte vectors of consecutive keys; for each key slot the
+// warp votes four masks -- class L, class G, region 0, region 2 -- and the
+// five outputs follow from them by mask logic: candidates (class B, compacted
+// with their values / positions), L keys outside region 0 and G keys
+// outside region 2 (listed by class), and the holes of regions 0 and 2
+// (positions there holding a foreign key).  A CTA votes SPL_SUB sub-steps
+// (masks kept in shared memory), adds its warps' counts and reserves each
+// output's slots with one global atomic per output; the warps then reload
+// the keys (from L2) and write, slot = warp base + running count + rank
+// among the lanes of the vote.  The order inside a list is irrelevant: every
+// listed key goes to some hole of its region.
+constexpr int SPL_BLOCK = 256;
+constexpr int SPL_WARPS = SPL_BLOCK / 32;
+constexpr int SPL_SUB = 8;                                // sub-steps per reservation
+template <typename C> struct SplShape {
+    static constexpr int VEC = 16 / (int)sizeof(C);     // keys per 16-byte vector
+    static constexpr int VECS = sizeof(C) == 8 ? 4 : 2;  // vectors per lane per sub-step
+    static constexpr int E = VEC * VECS;                  // keys per lane per sub-step (8)
+    static constexpr int WSUB = 32 * E;                   // keys per warp per sub-step
+    static constexpr int SUB = SPL_WARPS * WSUB;          // keys per CTA per sub-step
+    static constexpr int STEP = SPL_SUB * SUB;            // keys per reservation
+};
+
+template <typename C>
+__device__ __forceinline__ void spl_load(const C *keys, size_t n, size_t w0, int lane,
+                                         bool vec_ok, C (&raw)[SplShape<C>::E])
+{
+    using S = SplShape<C>;
+#pragma unroll
+    for (int v = 0; v < S::VECS; ++v) {
+        const size_t p0 = w0 + ((size_t)v * 32 + lane) * S::VEC;
+        if (vec_ok && p0 + S::VEC <= n) {
+            const uint4 q = *reinterpret_cast<const uint4 *>(keys + p0);
+            memcpy(&raw[v * S::VEC], &q, 16);
+        } else {
+#pragma unroll
+            for (int i = 0; i < S::VEC; ++i)
+                raw[v * S::VEC + i] = p0 + i < n ? keys[p0 + i] : C(0);
+        }
+    }
+}
+
+template <typename C, typename V>
+__global__ void __launch_bounds__(SPL_BLOCK, 2) sel_split_vote_kernel(SelArgs a, int lo, int bits)
+{
+    using S = SplShape<C>;
+    constexpr int E = S::E, VEC = S::VEC;
+    constexpr bool HAS_V = !std::is_same<V, uint8_t>::value;
+    __shared__ uint32_t sh[SEL_BINS];
+    __shared__ uint32_t s_mask[SPL_SUB][SPL_WARPS][E][4];   // L, G, region 0, region 2
+    __shared__ uint32_t s_cnt[SPL_WARPS][5];
+    __shared__ unsigned long long s_base[SPL_WARPS][5];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int nb = 1 << bits;
+    for (int i = tid; i < nb; i += SPL_BLOCK) sh[i] = 0;
+    __syncthreads();
+    const Codec<C> cx(a.xf);
+    const C pre = (C)a.st->prefix, msk = (C)a.st->mask;
+    const size_t b_lo = a.st->b_lo, b_hi = a.st->b_lo + a.st->b_n;
+    const C *keys = static_cast<const C *>(a.keys);
+    const V *vals = static_cast<const V *>(a.vals);
+    C *mis_k = static_cast<C *>(a.mis_k);
+    V *mis_v = static_cast<V *>(a.mis_v);
+    C *cand = static_cast<C *>(a.cand);
+    const size_t n = a.n;
+    const bool vec_ok = (reinterpret_cast<uintptr_t>(keys) & 15) == 0;
+    const uint32_t lt = (1u << lane) - 1u, bit = 1u << lane;
+    const size_t rs[3] = {0, b_lo, b_hi};
+    // output q: 0 = list L, 1 = list G, 2 = candidates, 3 = holes of region 0,
+    // 4 = holes of region 2
+    auto outputs = [&](const uint32_t (&m)[4], uint32_t act, uint32_t (&o)[5]) {
+        o[0] = m[0] & ~m[2];
+        o[1] = m[1] & ~m[3];
+        o[2] = act & ~(m[0] | m[1]);
+        o[3] = m[2] & ~m[0];
+        o[4] = m[3] & ~m[1];
+    };
+    auto pos = [&](size_t w0, int e) {
+        return w0 + ((size_t)(e / VEC) * 32 + lane) * VEC + (e % VEC);
+    };
+    for (size_t s0 = (size_t)blockIdx.x * S::STEP; s0 < n; s0 += (size_t)gridDim.x * S::STEP) {
+        // ---- vote every sub-step; masks to shared memory, counts per warp
+        uint32_t tot[5] = {0, 0, 0, 0, 0};
+        C raw[E], nxt[E];
+        spl_load<C>(keys, n, s0 + (size_t)warp * S::WSUB, lane, vec_ok, nxt);
+#pragma unroll 1
+        for (int sub = 0; sub < SPL_SUB; ++sub) {
+            const size_t w0 = s0 + (size_t)sub * S::SUB + (size_t)warp * S::WSUB;
+#pragma unroll
+            for (int e = 0; e < E; ++e) raw[e] = nxt[e];
+            if (sub + 1 < SPL_SUB) spl_load<C>(keys, n, w0 + S::SUB, lane, vec_ok, nxt);
+#pragma unroll
+            for (int e = 0; e < E; ++e) {
+                const size_t p = pos(w0, e);
+                const bool in = p < n;
+                const C c = cx.to(raw[e]);
+                const C top = (C)(c & msk);
+                uint32_t m[4];
+                m[0] = __ballot_sync(0xffffffffu, in && top < pre);
+                m[1] = __ballot_sync(0xffffffffu, in && top > pre);
+                m[2] = __ballot_sync(0xffffffffu, in && p < b_lo);
+                m[3] = __ballot_sync(0xffffffffu, in && p >= b_hi);
+                const uint32_t act = __ballot_sync(0xffffffffu, in);
+                if (in && top == pre) atomicAdd(&sh[uint32_t(c >> lo) & (uint32_t)(nb - 1)], 1u);
+                if (a.op == SOP_ARG && in && (p < b_lo || p >= b_hi)) a.out_idx[p] = p;
+                if (lane < 4) s_mask[sub][warp][e][lane] = m[lane];
+                uint32_t o[5];
+                outputs(m, act, o);
+#pragma unroll
+                for (int q = 0; q < 5; ++q) tot[q] += __popc(o[q]);
+            }
+        }
+        uint32_t mine = tot[0];
+#pragma unroll
+        for (int q = 1; q < 5; ++q)
+            if (lane == q) mine = tot[q];
+        if (lane < 5) s_cnt[warp][lane] = mine;
+        __syncthreads();
+        // ---- one reservation per output for the CTA's step
+        if (tid < 5) {
+            uint32_t sum = 0;
+            for (int w = 0; w < SPL_WARPS; ++w) sum += s_cnt[w][tid];
+            unsigned long long b = 0;
+            if (sum) {
+                if (tid == 2) b = atomicAdd(&a.st->cand_n, (unsigned long long)sum);
+                else if (tid < 2) b = atomicAdd(&a.st->nmis[tid == 0 ? 0 : 2], sum);
+                else b = atomicAdd(&a.st->nhole[tid == 3 ? 0 : 2], sum);
+            }
+            for (int w = 0; w < SPL_WARPS; ++w) {
+                s_base[w][tid] = b;
+                b += s_cnt[w][tid];
+            }
+        }
+        __syncthreads();
+        // ---- reload (L2) and write
+        unsigned long long run[5];
+#pragma unroll
+        for (int q = 0; q < 5; ++q) run[q] = s_base[warp][q];
+#pragma unroll 1
+        for (int sub = 0; sub < SPL_SUB; ++sub) {
+            const size_t w0 = s0 + (size_t)sub * S::SUB + (size_t)warp * S::WSUB;
+            if (w0 >= n) break;
+            spl_load<C>(keys, n, w0, lane, vec_ok, raw);
+#pragma unroll
+            for (int e = 0; e < E; ++e) {
+                const size_t p = pos(w0, e);
+                const uint32_t act = __ballot_sync(0xffffffffu, p < n);
+                uint32_t m[4];
+#pragma unroll
+                for (int i = 0; i < 4; ++i) m[i] = s_mask[sub][warp][e][i];
+                uint32_t o[5];
+                outputs(m, act, o);
+                if (o[2] & bit) {
+                    const unsigned long long at = run[2] + __popc(o[2] & lt);
+                    if (at < n) {
+                        cand[at] = cx.to(raw[e]);
+                        if (a.op == SOP_ARG) static_cast<uint32_t *>(a.cand_p)[at] = (uint32_t)p;
+                        else if constexpr (HAS_V)
+                            if (a.op == SOP_KV) static_cast<V *>(a.cand_p)[at] = vals[p];
+                    }
+                }
+#pragma unroll
+                for (int x = 0; x < 2; ++x) {
+                    if (o[x] & bit) {
+                        const unsigned long long at = rs[2 * x] + run[x] + __popc(o[x] & lt);
+                        if (at < n) {
+                            if (a.op == SOP_ARG) {
+                                reinterpret_cast<uint32_t *>(a.mis_v)[at] = (uint32_t)p;
+                            } else {
+                                mis_k[at] = raw[e];
+                                if constexpr (HAS_V)
+                                    if (a.op == SOP_KV) mis_v[at] = vals[p];
+                            }
+                        }
+                    }
+                    if (o[3 + x] & bit) {
+                        const unsigned long long at = rs[2 * x] + run[3 + x] + __popc(o[3 + x] & lt);
+                        if (at < n) a.holes[at] = (uint32_t)p;
+                    }
+                }
+#pragma unroll
+                for (int q = 0; q < 5; ++q) run[q] += __popc(o[q]);
+            }
+        }
+        __syncthreads();   // s_mask / s_cnt / s_base are rewritten by the next step
+    }
+    __syncthreads();
+    for (int i = tid; i < nb; i += SPL_BLOCK)
+        if (sh[i]) atomicAdd(&a.st->hist[i], sh[i]);
+}
+
 // B's region rewritten from the candidates, partitioned around K:
 // [b_lo, cl) < K, [cl, cl + ce) == K, [cl + ce, b_lo + b_n) > K.  Same chunk
 // and slot reservation scheme as the split pass, over the candidate list.
@@ -653,8 +846,11 @@ static int select_launch(int op, KeyXform xf, void *keys, void *vals, uint64_t *
         if (r == 1) {
             // one read of every key: candidates, their next-digit histogram,
             // and the L / G lists and holes
+            const int sg = (int)std::max<size_t>(
+                1, std::min<size_t>((n + SplShape<C>::STEP - 1) / SplShape<C>::STEP,
+                                    (size_t)sms * 4));
             XSS_LAUNCH(PK_SEL_COLLECT, s,
-                       (sel_split_kernel<C, V, false><<<grid, 256, 0, s>>>(a, lo, bits)));
+                       (sel_split_vote_kernel<C, V><<<sg, SPL_BLOCK, 0, s>>>(a, lo, bits)));
         } else {
             // round 0 reads every key; later rounds only the candidates
             const int g = r >= 2 ? std::max(1, grid / 4) : grid;

@@ -13,9 +13,10 @@
 #define XSS_CFG_K16 320, 20, 3, 16, 2, 1, 0
 #endif
 
-// K32: 320,20,3,8,2,1,0 3.679 ms; 320,20,3,16,2,1,0 3.773 ms; 512,16,2,8,2,1,0 3.744 ms; 384,16,3,8,2,1,0 3.697 ms; 256,24,3,8,2,1,0 3.758 ms; 256,16,4,8,2,1,0 4.172 ms; 320,16,4,8,2,1,0 4.203 ms
+// K32 (ranks packed two per register): 320,20,3,8,2,1,0 3.598 ms; 320,24,3,8,2,1,0 3.372 ms; 320,28,2,8,2,1,0 3.738 ms;
+// 320,32,2,8,2,1,0 3.513 ms; 320,40,2,8,2,1,0 5.198 ms; 384,32,2,8,2,1,0 3.323 ms; 256,40,2,8,2,1,0 3.788 ms; 256,32,3,8,2,1,0 4.101 ms
 #ifndef XSS_CFG_K32
-#define XSS_CFG_K32 320, 20, 3, 8, 2, 1, 0
+#define XSS_CFG_K32 384, 32, 2, 8, 2, 1, 0
 #endif
 
 // K64: 512,16,1,16,2,1,1 10.686 ms; 512,20,1,16,2,1,1 9.931 ms; 512,24,1,16,2,1,1 9.505 ms; 768,16,1,16,2,1,1 10.688 ms
@@ -23,19 +24,21 @@
 #define XSS_CFG_K64 512, 24, 1, 16, 2, 1, 1
 #endif
 
-// K32V32: 512,14,1,16,2,1,1 5.926 ms; 512,20,1,16,2,1,1 5.179 ms; 768,14,1,16,2,1,1 6.045 ms
+// K32V32: 512,14,1,16,2,1,1 5.926 ms; 512,20,1,16,2,1,1 5.173 ms; 768,14,1,16,2,1,1 6.045 ms; 512,24,1,16,2,1,1 4.954 ms
 #ifndef XSS_CFG_K32V32
-#define XSS_CFG_K32V32 512, 20, 1, 16, 2, 1, 1
+#define XSS_CFG_K32V32 512, 24, 1, 16, 2, 1, 1
 #endif
 
-// K64V64: 512,11,1,8,2,1,1 16.375 ms; 512,12,1,8,2,1,1 15.918 ms; 640,10,1,8,2,1,1 15.906 ms; 768,8,1,8,2,1,1 16.529 ms; 384,16,1,8,2,1,1 16.101 ms; 512,12,1,16,2,1,1 16.037 ms
+// K64V64: 512,11,1,8,2,1,1 16.375 ms; 512,12,1,8,2,1,1 15.918 ms; 640,10,1,8,2,1,1 15.906 ms; 768,8,1,8,2,1,1 16.529 ms;
+// 384,16,1,8,2,1,1 16.101 ms; 512,12,1,16,2,1,1 16.037 ms; 576,11,1,8,2,1,1 15.785 ms
 #ifndef XSS_CFG_K64V64
-#define XSS_CFG_K64V64 640, 10, 1, 8, 2, 1, 1
+#define XSS_CFG_K64V64 576, 11, 1, 8, 2, 1, 1
 #endif
 
-// DEFAULT: 512,14,1,8,2,1,1 13.262 ms; 512,16,1,8,2,1,1 12.633 ms; 640,12,1,8,2,1,1 13.195 ms; 768,10,1,8,2,1,1 13.409 ms
+// DEFAULT: 512,14,1,8,2,1,1 13.262 ms; 512,16,1,8,2,1,1 12.557 ms; 640,12,1,8,2,1,1 13.195 ms; 768,10,1,8,2,1,1 13.409 ms;
+// 512,17,1,8,2,1,1 12.488 ms
 #ifndef XSS_CFG_DEFAULT
-#define XSS_CFG_DEFAULT 512, 16, 1, 8, 2, 1, 1
+#define XSS_CFG_DEFAULT 512, 17, 1, 8, 2, 1, 1
 #endif
 
 // K32_MID: 512,16,2,16,2,1,0 0.082 ms; 256,16,3,16,2,1,0 0.093 ms; 256,8,4,16,2,1,0 0.101 ms
