@@ -183,7 +183,7 @@ class KeyValueSort(Workload):
     def bytes_per_pass(self):           # read + write of key and value
         return 2 * self.n * (self.kb + self.vb)
 
-    def bytes_model(self):              # survey model: n(kb + 2P(kb+vb))
+    def bytes_model(self):              # fixed model: n(kb + 2P(kb+vb))
         return self.n * (self.kb + 2 * self.passes() * (self.kb + self.vb))
 
     # host-pointer (e2e) path
@@ -1136,12 +1136,12 @@ def cpu_baseline(wl, budget_s=12.0, sample_n=1 << 24):
                       f"median of {len(times)} runs"}
 
 
-# The reference's own numbers for these workloads, measured while surveying it
+# The reference's own numbers for these workloads, measured on an x86 host
 # (built from its sources with g++ 13.3, AVX-512 dispatch, OpenMP on 8 threads of
 # an x86 Xeon @ 2.70 GHz; single wall-clock runs).  Its SIMD code needs x86-64
 # and its sources do not travel with this repository, so on other hosts the
 # reference arm times the oracle's port and reports these beside it.
-SURVEY_REFERENCE = {
+X86_REFERENCE_FIGURES = {
     "keyvalue_qsort": {"value": 0.1175, "unit": "Gkeys/s", "n": 1 << 28,
                        "what": "keyvalue_qsort<int64,uint64> ascending, 2^28 in 2.28 s"},
     "argsort_i64": {"value": 0.0225, "unit": "Gkeys/s", "n": 1 << 28,
@@ -1154,7 +1154,7 @@ SURVEY_REFERENCE = {
                     "what": "argsort<double> hasnan descending 1% NaN (scalar fallback), "
                             "2^24 in 5.39 s"},
 }
-SURVEY_HOST = "x86 survey container: 8 threads (OpenMP), Intel Xeon @ 2.70 GHz, AVX-512"
+X86_REFERENCE_HOST = "x86 host: 8 threads (OpenMP), Intel Xeon @ 2.70 GHz, AVX-512"
 
 
 def reference_arm(args):
@@ -1230,11 +1230,11 @@ def reference_arm(args):
                                               else "inside the timed region"},
             "e2e": {"value": val, "unit": "Gkeys/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
-    if args.workload in SURVEY_REFERENCE:
-        line["reference_survey_host"] = {**SURVEY_REFERENCE[args.workload],
-                                         "host": SURVEY_HOST,
-                                         "source": "measured while surveying the reference; "
-                                                   "not on this host"}
+    if args.workload in X86_REFERENCE_FIGURES:
+        line["reference_x86_host"] = {**X86_REFERENCE_FIGURES[args.workload],
+                                      "host": X86_REFERENCE_HOST,
+                                      "source": "the reference built and run on an x86 host; "
+                                                "not on this host"}
     print(json.dumps(line), flush=True)
 
 

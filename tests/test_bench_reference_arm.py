@@ -55,4 +55,4 @@ def test_reference_arm_times_the_full_workload_when_it_fits():
     assert line["config"]["same_config"] is True
     assert line["cpu_baseline"]["sample"] == f"{1 << 20} keys per step"
     assert line["cpu_baseline"]["input_restore"] == "outside the timed region"
-    assert line["reference_survey_host"]["value"] > 0
+    assert line["reference_x86_host"]["value"] > 0

@@ -28,7 +28,7 @@ def test_candidate_lines_are_well_formed():
             block, items, minb, lb, rank, persist, dpt = f
             assert block % 32 == 0 and 256 <= block <= 1024
             assert items >= 1 and minb >= 1 and lb in (8, 16, 32)
-            assert rank in (0, 1, 2) and persist in (0, 1, 2) and dpt in (0, 1, 2, 4, 12, 14)
+            assert rank in (0, 1, 2) and persist in (0, 1, 2, 3) and dpt in (0, 1, 2, 4, 12, 14)
 
 
 def test_committed_header_covers_every_class():

@@ -64,7 +64,10 @@ __device__ __forceinline__ void *pick3(void *const (&b)[3], int i)
 //                 warp (shared atomics that meet at one address within a warp
 //                 instruction return in lane order; see rank_order_verified)
 //   PERSIST:      0 = one CTA per tile, 1 = resident CTAs with TMA prefetch,
-//                 2 = resident CTAs with ordinary loads (one staging buffer)
+//                 2 = resident CTAs with ordinary loads (one staging buffer),
+//                 3 = resident CTAs holding two tiles, the next one counted
+//                 and published before the current one's look-back
+//                 (onesweep_pipe_kernel; RANK must be 2, DPT is unused)
 //   DPT:          look-back placement.  0: after ranking, one digit per
 //                 thread; 1, 2, 4: right after the counts, by 256 / DPT
 //                 threads with DPT digits each while the other warps rank;
@@ -694,6 +697,293 @@ __global__ void __launch_bounds__(BLOCK, MINB) onesweep_persist_kernel(RadixArgs
         else
             onesweep_persist_body<C, V, BLOCK, ITEMS, LB, RANK, DPT, PF, ROLE_MID>(
                 a, pass, pd, ps, s_tile, s_bar, s_dyn);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Pipelined resident form (PERSIST 3).  A CTA holds two tiles: the current
+// one, ranked and staged in the staging buffer, and the next one, landing in
+// the landing buffer.  Each iteration reads the next tile into registers,
+// counts it, starts the copy of the tile after it into the landing buffer
+// (now free), publishes the next tile's aggregate, and only then walks back
+// for the current tile; it scatters the current tile and stages the next.  The walk thus starts a
+// count and a scan later than in pass_tile (its predecessors are further
+// along, so it needs fewer round trips), and a tile's aggregate goes out
+// soon after its data lands instead of after the previous tile's walk and
+// scatter.  Ranks come from the count atomics (RANK 2) in every pass.
+// Deadlock-free as the other forms: tiles are claimed in increasing order,
+// and the CTA holding the lowest unfinished tile has every predecessor's
+// inclusive prefix available.
+template <int BLOCK> struct PipeSmem {
+    uint32_t wh[(BLOCK / 32) * RADIX];   // per-warp counts, then per-warp offsets
+    uint32_t cl[2][RADIX];               // per held tile: count | local start << 16
+    int32_t off[RADIX];                  // global offset - local start, current tile
+    uint32_t scan[BLOCK / 32];
+};
+
+template <typename C, typename V, int BLOCK, int ITEMS, int LB, int ROLE>
+__device__ __forceinline__ void onesweep_pipe_body(const RadixArgs &a, int pass,
+                                                   const PassDesc &pd, PipeSmem<BLOCK> &ps,
+                                                   uint32_t (&s_tile)[2], uint64_t (&s_bar)[2],
+                                                   unsigned char *s_dyn)
+{
+    constexpr int WARPS = BLOCK / 32;
+    constexpr int TILE = BLOCK * ITEMS;
+    constexpr bool HAS_V = !std::is_same<V, NoVal>::value;
+    using VS = typename std::conditional<HAS_V, V, uint8_t>::type;
+    constexpr size_t VSZ = HAS_V ? sizeof(V) : 0;
+    static_assert(TILE < 65536, "ranks, counts and local starts fit 16 bits");
+    const Codec<C> cx(a.xf);
+    C *const s_k0 = reinterpret_cast<C *>(s_dyn);
+    VS *const s_v0 = reinterpret_cast<VS *>(s_dyn + 2 * TILE * sizeof(C));
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const uint32_t n = (uint32_t)a.n;
+    const uint32_t num_tiles = a.num_tiles;
+    const int shift = pass * RADIX_BITS;
+    const C *ksrc = static_cast<const C *>(pick3(a.kbuf, pd.src));
+    C *kdst = static_cast<C *>(pick3(a.kbuf, pd.dst));
+    const V *vsrc = nullptr;
+    V *vdst = nullptr;
+    if constexpr (HAS_V) {
+        vsrc = static_cast<const V *>(pick3(a.vbuf, pd.vsrc));
+        vdst = static_cast<V *>(pick3(a.vbuf, pd.vdst));
+    }
+    const bool load_vals = HAS_V && !pd.gen_idx;
+    const bool tma = (reinterpret_cast<uintptr_t>(ksrc) & 15) == 0 &&
+                     (!load_vals || (reinterpret_cast<uintptr_t>(vsrc) & 15) == 0);
+    const uint32_t tile_bytes = TILE * (uint32_t)(sizeof(C) + (load_vals ? VSZ : 0));
+    uint32_t *const st_pass = a.status + (size_t)pass * num_tiles * RADIX;
+    const uint32_t *const gstart = a.hdr->start[pass];
+    uint32_t *const wh = ps.wh + warp * RADIX;
+    const uint32_t local0 = (uint32_t)warp * (ITEMS * 32) + lane;
+
+    auto issue = [&](uint32_t t, int b) {
+        const size_t base = (size_t)t * TILE;
+        mbar_arrive_expect_tx(&s_bar[b], tile_bytes);
+        bulk_load(s_k0 + b * TILE, ksrc + base, TILE * sizeof(C), &s_bar[b]);
+        if constexpr (HAS_V)
+            if (load_vals) bulk_load(s_v0 + b * TILE, vsrc + base, TILE * sizeof(VS), &s_bar[b]);
+    };
+    auto by_tma = [&](uint32_t t) { return tma && t < num_tiles && (size_t)t * TILE + TILE <= n; };
+    // claim a tile and start its copy into the landing buffer (0)
+    auto claim_next = [&]() {
+        if (tid == 0) {
+            const uint32_t t1 = atomicAdd(&a.hdr->tile_ctr[pass], 1u);
+            s_tile[0] = t1;
+            if (by_tma(t1)) {
+                fence_proxy_async_smem();
+                issue(t1, 0);
+            }
+        }
+    };
+
+    uint32_t parity[2] = {0u, 0u};
+    C key[ITEMS];
+    VS val[ITEMS];
+    uint32_t wrank[(ITEMS + 1) / 2];
+    // tile t (data in buffer b) into registers; false: its copy never landed
+    // (the error word is set), and the CTA stops
+    auto load_tile = [&](uint32_t t, int b) -> bool {
+        const uint32_t tile_base = t * (uint32_t)TILE;
+        if (by_tma(t)) {
+            const bool landed = mbar_wait_bounded(&s_bar[b], parity[b], a.err);
+            if (__syncthreads_or(!landed)) return false;
+            parity[b] ^= 1u;
+            const C *sk = s_k0 + b * TILE;
+#pragma unroll
+            for (int j = 0; j < ITEMS; ++j) {
+                const C x = sk[local0 + j * 32];
+                key[j] = (ROLE & ROLE_FIRST) ? cx.to(x) : x;
+            }
+            if constexpr (HAS_V) {
+                const VS *sv = s_v0 + b * TILE;
+#pragma unroll
+                for (int j = 0; j < ITEMS; ++j)
+                    val[j] = pd.gen_idx ? VS(tile_base + local0 + j * 32) : sv[local0 + j * 32];
+            }
+        } else {
+#pragma unroll
+            for (int j = 0; j < ITEMS; ++j) {
+                const uint32_t idx = tile_base + local0 + j * 32;
+                if (idx < n) {
+                    const C x = ksrc[idx];
+                    key[j] = (ROLE & ROLE_FIRST) ? cx.to(x) : x;
+                } else {
+                    key[j] = C(~C(0));
+                }
+            }
+            if constexpr (HAS_V) {
+#pragma unroll
+                for (int j = 0; j < ITEMS; ++j) {
+                    const uint32_t idx = tile_base + local0 + j * 32;
+                    val[j] = pd.gen_idx ? VS(idx) : (idx < n ? vsrc[idx] : VS(0));
+                }
+            }
+        }
+        return true;
+    };
+    // per-warp digit counts; each key keeps its rank in its warp
+    auto count = [&]() {
+#pragma unroll
+        for (int j = 0; j < ITEMS; ++j) {
+            const uint32_t r = atomicAdd(&wh[uint32_t(key[j] >> shift) & (RADIX - 1)], 1u);
+            if (j & 1) wrank[j >> 1] |= r << 16;
+            else wrank[j >> 1] = r;
+            __syncwarp();
+        }
+    };
+    // (after a barrier) publish tile t's counts, scan them, per-warp offsets
+    auto publish_scan = [&](uint32_t t, int slot) {
+        uint32_t c = 0;
+        if (tid < RADIX) {
+#pragma unroll
+            for (int w = 0; w < WARPS; ++w) c += ps.wh[w * RADIX + tid];
+            st_relaxed_u32(st_pass + (size_t)t * RADIX + tid, (t == 0 ? FLAG_PRE : FLAG_AGG) | c);
+        }
+        uint32_t total;
+        const uint32_t ls = block_excl_scan<BLOCK>(c, ps.scan, total);
+        if (tid < RADIX) {
+            uint32_t run = ls;
+#pragma unroll
+            for (int w = 0; w < WARPS; ++w) {
+                const uint32_t x = ps.wh[w * RADIX + tid];
+                ps.wh[w * RADIX + tid] = run;
+                run += x;
+            }
+            ps.cl[slot][tid] = c | (ls << 16);
+        }
+    };
+    // (tid < RADIX) tile t's global offsets; its inclusive prefixes go out
+    auto walk = [&](uint32_t t, int slot) {
+        uint32_t excl[1] = {0};
+        const uint32_t cl = ps.cl[slot][tid];
+        if (t > 0) {
+            lookback_excl<LB, 1>(st_pass, t, 0u, tid, a.err, excl);
+            st_relaxed_u32(st_pass + (size_t)t * RADIX + tid,
+                           FLAG_PRE | ((excl[0] + (cl & 0xFFFFu)) & COUNT_MASK));
+        }
+        ps.off[tid] = (int32_t)(gstart[tid] + excl[0]) - (int32_t)(cl >> 16);
+    };
+    auto stage = [&](int b) {
+        C *sk = s_k0 + b * TILE;
+        VS *sv = s_v0 + b * TILE;
+#pragma unroll
+        for (int j = 0; j < ITEMS; ++j) {
+            const uint32_t p = wh[uint32_t(key[j] >> shift) & (RADIX - 1)] +
+                               ((wrank[j >> 1] >> (16 * (j & 1))) & 0xFFFFu);
+            sk[p] = key[j];
+            if constexpr (HAS_V) sv[p] = val[j];
+        }
+    };
+    auto scatter = [&](uint32_t t, int b) {
+        const C *sk = s_k0 + b * TILE;
+        const VS *sv = s_v0 + b * TILE;
+        const uint32_t valid = min((uint32_t)TILE, n - t * (uint32_t)TILE);
+#pragma unroll
+        for (int m = 0; m < ITEMS; ++m) {
+            const uint32_t i = tid + m * BLOCK;
+            if (i < valid) {
+                const C c = sk[i];
+                const uint32_t d = uint32_t(c >> shift) & (RADIX - 1);
+                const uint32_t g = (uint32_t)(ps.off[d] + (int32_t)i);
+                if (g < n) {
+                    if (!pd.skip_keys) {
+                        if constexpr ((ROLE & ROLE_LAST) != 0) kdst[g] = cx.from_canon(c);
+                        else kdst[g] = c;
+                    }
+                    if constexpr (HAS_V) {
+                        if (pd.out_idx) a.out_idx[g] = (uint64_t)sv[i];
+                        else vdst[g] = sv[i];
+                    }
+                } else {
+                    atomicOr(a.err, XSS_DEVERR_BOUNDS);  // only after a look-back timeout
+                }
+            }
+        }
+    };
+    auto clear_wh = [&]() {
+        for (int i = tid; i < WARPS * RADIX; i += BLOCK) ps.wh[i] = 0;
+    };
+
+    // ---- prologue: the first tile counted, published, staged
+    clear_wh();
+    if (tid == 0) {
+        mbar_init(&s_bar[0], 1);
+        fence_mbar_init();
+        const uint32_t t0 = atomicAdd(&a.hdr->tile_ctr[pass], 1u);
+        s_tile[0] = t0;
+        if (by_tma(t0)) issue(t0, 0);
+    }
+    __syncthreads();
+    int slot = 0;                             // count / start slot of the current tile
+    uint32_t t = s_tile[0];
+    if (t >= num_tiles) return;
+    if (!load_tile(t, 0)) return;
+    count();
+    __syncthreads();                          // the landing buffer is read
+    claim_next();
+    publish_scan(t, slot);
+    __syncthreads();
+    stage(1);
+    __syncthreads();
+
+    for (;;) {
+        const uint32_t nxt = s_tile[0];
+        const bool have_next = nxt < num_tiles;   // uniform across the CTA
+        clear_wh();
+        __syncthreads();
+        if (have_next) {
+            if (!load_tile(nxt, 0)) {
+                // the next tile's copy never landed: finish the current tile
+                // (its walk may give up too; the error word is already set)
+                if (tid < RADIX) walk(t, slot);
+                __syncthreads();
+                scatter(t, 1);
+                return;
+            }
+            count();
+        }
+        __syncthreads();                      // the landing buffer is read
+        if (have_next) {
+            claim_next();
+            publish_scan(nxt, slot ^ 1);
+        }
+        if (tid < RADIX) walk(t, slot);
+        __syncthreads();
+        scatter(t, 1);
+        __syncthreads();
+        if (!have_next) break;
+        stage(1);
+        __syncthreads();
+        t = nxt;
+        slot ^= 1;
+    }
+}
+
+template <typename C, typename V, int BLOCK, int ITEMS, int MINB, int LB>
+__global__ void __launch_bounds__(BLOCK, MINB) onesweep_pipe_kernel(RadixArgs a, int pass)
+{
+    static_assert(BLOCK >= RADIX, "one thread per digit");
+    const PassDesc pd = a.hdr->desc[pass];
+    if (!pd.active) return;
+    __shared__ PipeSmem<BLOCK> ps;
+    __shared__ uint32_t s_tile[2];
+    __shared__ __align__(8) uint64_t s_bar[2];
+    extern __shared__ __align__(128) unsigned char s_dyn[];
+    if (pd.first) {
+        if (pd.last)
+            onesweep_pipe_body<C, V, BLOCK, ITEMS, LB, ROLE_FIRST | ROLE_LAST>(a, pass, pd, ps,
+                                                                              s_tile, s_bar, s_dyn);
+        else
+            onesweep_pipe_body<C, V, BLOCK, ITEMS, LB, ROLE_FIRST>(a, pass, pd, ps, s_tile, s_bar,
+                                                                   s_dyn);
+    } else {
+        if (pd.last)
+            onesweep_pipe_body<C, V, BLOCK, ITEMS, LB, ROLE_LAST>(a, pass, pd, ps, s_tile, s_bar,
+                                                                  s_dyn);
+        else
+            onesweep_pipe_body<C, V, BLOCK, ITEMS, LB, ROLE_MID>(a, pass, pd, ps, s_tile, s_bar,
+                                                                 s_dyn);
     }
 }
 

@@ -433,6 +433,32 @@ static int resident_passes(const RadixArgs &a, int sms, cudaStream_t s, const La
     return XSS_OK;
 }
 
+// Pipelined resident CTAs (two tiles held per CTA) for every active pass.
+template <typename C, typename V, int BLOCK, int ITEMS, int MINB, int LB>
+static int pipe_passes(const RadixArgs &a, int sms, cudaStream_t s, const LaunchOpts &o)
+{
+    constexpr size_t TILE = (size_t)BLOCK * ITEMS;
+    constexpr bool HAS_V = !std::is_same<V, NoVal>::value;
+    const size_t smem = 2 * TILE * (sizeof(C) + (HAS_V ? sizeof(V) : 0));
+    auto kern = onesweep_pipe_kernel<C, V, BLOCK, ITEMS, MINB, LB>;
+    int rc = set_max_dyn_smem((const void *)kern, smem);
+    if (rc) return rc;
+    static std::atomic<int> per_sm_cached{0};   // same GPU model on every device
+    int per_sm = per_sm_cached.load(std::memory_order_relaxed);
+    if (!per_sm) {
+        int v = 0;
+        XSS_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, kern, BLOCK, smem));
+        per_sm = std::max(v, 1);
+        per_sm_cached.store(per_sm, std::memory_order_relaxed);
+    }
+    const uint32_t grid = (uint32_t)std::min<size_t>(a.num_tiles, (size_t)per_sm * sms);
+    for (int p = 0; p < a.passes; ++p) {
+        XSS_LAUNCH_OPT(o, PK_ONESWEEP, s, kern<<<grid, BLOCK, smem, s>>>(a, p));
+        XSS_CUDA_TRY(cudaGetLastError());
+    }
+    return XSS_OK;
+}
+
 // One CTA per tile for every active pass.
 template <typename C, typename V, int BLOCK, int ITEMS, int MINB, int LB, int RANK, int DPT>
 static int tile_passes(const RadixArgs &a, cudaStream_t s, const LaunchOpts &o)
@@ -522,7 +548,10 @@ static int onesweep_launch_cls(int op, KeyXform xf, void *keys, void *vals, uint
     XSS_CUDA_TRY(cudaGetLastError());
 
     int rc = XSS_OK;
-    if constexpr (Cfg::PERSIST == 1)
+    if constexpr (Cfg::PERSIST == 3) {
+        static_assert(RANK == 2, "the pipelined form ranks by the count atomic");
+        rc = pipe_passes<C, V, BLOCK, ITEMS, MINB, LB>(a, sms, s, o);
+    } else if constexpr (Cfg::PERSIST == 1)
         rc = resident_passes<C, V, BLOCK, ITEMS, MINB, LB, RANK, DPT, true>(a, sms, s, o);
     else if constexpr (Cfg::PERSIST == 2)
         rc = resident_passes<C, V, BLOCK, ITEMS, MINB, LB, RANK, DPT, false>(a, sms, s, o);

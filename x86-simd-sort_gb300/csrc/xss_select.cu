@@ -17,7 +17,10 @@
 // candidates.  With the exact k-th code K known, the candidates are written
 // back into B's region partitioned around K, and a last kernel moves the
 // listed L/G elements into the holes.  Only misplaced elements move, as in
-// an in-place quickselect partition, and the array is read twice.
+// an in-place quickselect partition, and the array is read twice.  When k
+// is far from both ends (about half of each side's keys misplaced) the split
+// instead writes every key once to a scratch copy -- L to its front, G to its
+// back -- and the outer regions are copied back (select_launch chooses).
 #include <algorithm>
 #include <cstring>
 #include <type_traits>
@@ -450,19 +453,9 @@ __global__ void __launch_bounds__(256) sel_split_kernel(SelArgs a, int lo, int b
     }
 }
 
-// The split pass for 32- and 64-bit keys (B is a bucket of codes sharing
-// the top digit, so its keys become candidates), by warp votes.  Every lane
-// loads SPL_VECS 16-byte vectors of consecutive keys; for each key slot the
-// warp votes four masks -- class L, class G, region 0, region 2 -- and the
-// five outputs follow from them by mask logic: candidates (class B, compacted
-// with their values / positions), L keys outside region 0 and G keys
-// outside region 2 (listed by class), and the holes of regions 0 and 2
-// (positions there holding a foreign key).  A CTA votes SPL_SUB sub-steps
-// (masks kept in shared memory), adds its warps' counts and reserves each
-// output's slots with one global atomic per output; the warps then reload
-// the keys (from L2) and write, slot = warp base + running count + rank
-// among the lanes of the vote.  The order inside a list is irrelevant: every
-// listed key goes to some hole of its region.
+// Shape of the out-of-place split (below): CTAs of SPL_BLOCK threads, each
+// lane loading 16-byte vectors of consecutive keys, SPL_SUB sub-steps per
+// slot reservation.
 constexpr int SPL_BLOCK = 256;
 constexpr int SPL_WARPS = SPL_BLOCK / 32;
 constexpr int SPL_SUB = 8;                                // sub-steps per reservation
@@ -476,13 +469,13 @@ template <typename C> struct SplShape {
 };
 
 template <typename C>
-__device__ __forceinline__ void spl_load(const C *keys, size_t n, size_t w0, int lane,
+__device__ __forceinline__ void spl_load(const C *keys, uint32_t n, uint32_t w0, int lane,
                                          bool vec_ok, C (&raw)[SplShape<C>::E])
 {
     using S = SplShape<C>;
 #pragma unroll
     for (int v = 0; v < S::VECS; ++v) {
-        const size_t p0 = w0 + ((size_t)v * 32 + lane) * S::VEC;
+        const uint32_t p0 = w0 + ((uint32_t)v * 32 + (uint32_t)lane) * S::VEC;
         if (vec_ok && p0 + S::VEC <= n) {
             const uint4 q = *reinterpret_cast<const uint4 *>(keys + p0);
             memcpy(&raw[v * S::VEC], &q, 16);
@@ -494,146 +487,296 @@ __device__ __forceinline__ void spl_load(const C *keys, size_t n, size_t w0, int
     }
 }
 
+// Sparse in-place split for k near either end of the array (32- and 64-bit
+// keys): few keys need recording -- the candidates (class B), the L / G keys
+// outside their regions and the holes they leave -- so each warp classifies
+// a 16-byte vector row per lane with a few instructions per key and moves on
+// unless some lane holds a key to record.  Only then does it vote the five
+// output masks of each key slot and reserve slots with one global atomic per
+// non-empty output (rare, so the counters see little contention).  Output
+// layout as the tag split above (lists and holes start at their region's
+// first position); argselect writes the identity of every position outside
+// B's region.
 template <typename C, typename V>
-__global__ void __launch_bounds__(SPL_BLOCK, 2) sel_split_vote_kernel(SelArgs a, int lo, int bits)
+__global__ void __launch_bounds__(256) sel_split_sparse_kernel(SelArgs a, int lo, int bits)
 {
     using S = SplShape<C>;
     constexpr int E = S::E, VEC = S::VEC;
     constexpr bool HAS_V = !std::is_same<V, uint8_t>::value;
     __shared__ uint32_t sh[SEL_BINS];
-    __shared__ uint32_t s_mask[SPL_SUB][SPL_WARPS][E][4];   // L, G, region 0, region 2
-    __shared__ uint32_t s_cnt[SPL_WARPS][5];
-    __shared__ unsigned long long s_base[SPL_WARPS][5];
+    const int tid = threadIdx.x, lane = tid & 31;
+    const int nb = 1 << bits;
+    for (int i = tid; i < nb; i += 256) sh[i] = 0;
+    __syncthreads();
+    const Codec<C> cx(a.xf);
+    const C pre = (C)a.st->prefix, msk = (C)a.st->mask;
+    const uint32_t n = (uint32_t)a.n;
+    const uint32_t b_lo = (uint32_t)a.st->b_lo, b_hi = (uint32_t)(a.st->b_lo + a.st->b_n);
+    const uint32_t rs[3] = {0u, b_lo, b_hi};
+    const C *keys = static_cast<const C *>(a.keys);
+    const V *vals = static_cast<const V *>(a.vals);
+    C *mis_k = static_cast<C *>(a.mis_k);
+    V *mis_v = static_cast<V *>(a.mis_v);
+    C *cand = static_cast<C *>(a.cand);
+    const bool vec_ok = (reinterpret_cast<uintptr_t>(keys) & 15) == 0;
+    const uint32_t lt = (1u << lane) - 1u, bit = 1u << lane;
+    const uint32_t lane0 = (uint32_t)lane * VEC;
+    const uint32_t wstride = gridDim.x * 8u * (uint32_t)S::WSUB;
+    for (uint32_t w0 = (blockIdx.x * 8u + (uint32_t)(tid >> 5)) * (uint32_t)S::WSUB; w0 < n;
+         w0 += wstride) {
+        C raw[E];
+        spl_load<C>(keys, n, w0, lane, vec_ok, raw);
+        uint32_t cls4 = 0, reg4 = 0;   // 2 bits per key slot
+        bool any = false;
+#pragma unroll
+        for (int e = 0; e < E; ++e) {
+            const uint32_t p = w0 + (uint32_t)(e / VEC) * (32 * VEC) + lane0 + (e % VEC);
+            const C top = (C)(cx.to(raw[e]) & msk);
+            const uint32_t cls = (uint32_t)(top >= pre) + (uint32_t)(top > pre);
+            const uint32_t reg = (uint32_t)(p >= b_lo) + (uint32_t)(p >= b_hi);
+            cls4 |= cls << (2 * e);
+            reg4 |= reg << (2 * e);
+            if (p < n) {
+                any |= cls != reg || cls == 1u;
+                if (a.op == SOP_ARG && reg != 1u) a.out_idx[p] = p;
+            }
+        }
+        if (!__any_sync(0xffffffffu, any)) continue;
+#pragma unroll 1
+        for (int e = 0; e < E; ++e) {
+            const uint32_t p = w0 + (uint32_t)(e / VEC) * (32 * VEC) + lane0 + (e % VEC);
+            const bool in = p < n;
+            const uint32_t cls = (cls4 >> (2 * e)) & 3u, reg = (reg4 >> (2 * e)) & 3u;
+            // outputs: 0 list L, 1 list G, 2 candidates, 3 holes of region 0, 4 of region 2
+            uint32_t m[5];
+            m[0] = __ballot_sync(0xffffffffu, in && cls == 0u && reg != 0u);
+            m[1] = __ballot_sync(0xffffffffu, in && cls == 2u && reg != 2u);
+            m[2] = __ballot_sync(0xffffffffu, in && cls == 1u);
+            m[3] = __ballot_sync(0xffffffffu, in && reg == 0u && cls != 0u);
+            m[4] = __ballot_sync(0xffffffffu, in && reg == 2u && cls != 2u);
+            if ((m[0] | m[1] | m[2] | m[3] | m[4]) == 0u) continue;
+            uint32_t base = 0;
+            if (lane < 5) {
+                const uint32_t c = __popc(lane == 0 ? m[0] : lane == 1 ? m[1] : lane == 2 ? m[2] : lane == 3 ? m[3] : m[4]);
+                if (c) {
+                    if (lane == 2) base = (uint32_t)atomicAdd(&a.st->cand_n, (unsigned long long)c);
+                    else if (lane < 2) base = rs[lane == 0 ? 0 : 2] + atomicAdd(&a.st->nmis[lane == 0 ? 0 : 2], c);
+                    else base = rs[lane == 3 ? 0 : 2] + atomicAdd(&a.st->nhole[lane == 3 ? 0 : 2], c);
+                }
+            }
+            uint32_t b[5];
+#pragma unroll
+            for (int q = 0; q < 5; ++q) b[q] = __shfl_sync(0xffffffffu, base, q);
+            if (!in) continue;
+            if (m[2] & bit) {
+                const C c = cx.to(raw[e]);
+                atomicAdd(&sh[uint32_t(c >> lo) & (uint32_t)(nb - 1)], 1u);
+                const uint32_t at = b[2] + __popc(m[2] & lt);
+                if (at < n) {
+                    cand[at] = c;
+                    if (a.op == SOP_ARG) static_cast<uint32_t *>(a.cand_p)[at] = p;
+                    else if constexpr (HAS_V)
+                        if (a.op == SOP_KV) static_cast<V *>(a.cand_p)[at] = vals[p];
+                }
+            }
+#pragma unroll
+            for (int x = 0; x < 2; ++x) {
+                if (m[x] & bit) {
+                    const uint32_t at = b[x] + __popc(m[x] & lt);
+                    if (at < n) {
+                        if (a.op == SOP_ARG) {
+                            reinterpret_cast<uint32_t *>(a.mis_v)[at] = p;
+                        } else {
+                            mis_k[at] = raw[e];
+                            if constexpr (HAS_V)
+                                if (a.op == SOP_KV) mis_v[at] = vals[p];
+                        }
+                    }
+                }
+                if (m[3 + x] & bit) {
+                    const uint32_t at = b[3 + x] + __popc(m[3 + x] & lt);
+                    if (at < n) a.holes[at] = p;
+                }
+            }
+        }
+    }
+    __syncthreads();
+    for (int i = tid; i < nb; i += 256)
+        if (sh[i]) atomicAdd(&a.st->hist[i], sh[i]);
+}
+
+// Out-of-place three-way split for 32- and 64-bit keys: every key of class L
+// goes to the front of a scratch copy of the array ([0, b_lo)), every key of
+// class G to its back ([b_hi, n)), and B's keys become candidates (codes,
+// with values or positions).  Argselect writes the positions of L and G
+// straight into its output instead of the scratch copy.  For each key slot
+// the warp votes two masks (class L, class G; class B is the rest); a CTA
+// votes SPL_SUB sub-steps (masks kept in shared memory), adds its warps'
+// counts and reserves each output's slots with one global atomic per output,
+// then reloads the keys (from L2) and writes each once, slot = warp base +
+// running count + rank among the lanes of the vote.  No hole lists are kept;
+// sel_copyback_kernel then moves the scratch regions into the array.
+// The values of the keys spl_load read (same key slots), with vector loads
+// where the value array is aligned to a row of VEC values.
+template <typename C, typename V>
+__device__ __forceinline__ void spl_load_vals(const V *vals, uint32_t n, uint32_t w0, int lane,
+                                              bool vec_ok, V (&out)[SplShape<C>::E])
+{
+    using S = SplShape<C>;
+    constexpr int VB = S::VEC * (int)sizeof(V);   // bytes of one row: 4 .. 32
+#pragma unroll
+    for (int v = 0; v < S::VECS; ++v) {
+        const uint32_t p0 = w0 + ((uint32_t)v * 32 + (uint32_t)lane) * S::VEC;
+        if (vec_ok && p0 + S::VEC <= n && VB >= 4) {
+            if constexpr (VB == 32) {
+                const uint4 *q = reinterpret_cast<const uint4 *>(vals + p0);
+                const uint4 x = q[0], y = q[1];
+                memcpy(&out[v * S::VEC], &x, 16);
+                memcpy(reinterpret_cast<char *>(&out[v * S::VEC]) + 16, &y, 16);
+            } else if constexpr (VB == 16) {
+                const uint4 x = *reinterpret_cast<const uint4 *>(vals + p0);
+                memcpy(&out[v * S::VEC], &x, 16);
+            } else if constexpr (VB == 8) {
+                const uint2 x = *reinterpret_cast<const uint2 *>(vals + p0);
+                memcpy(&out[v * S::VEC], &x, 8);
+            } else {
+                const uint32_t x = *reinterpret_cast<const uint32_t *>(vals + p0);
+                memcpy(&out[v * S::VEC], &x, 4);
+            }
+        } else {
+#pragma unroll
+            for (int i = 0; i < S::VEC; ++i)
+                out[v * S::VEC + i] = p0 + i < n ? vals[p0 + i] : V(0);
+        }
+    }
+}
+
+template <typename C, typename V>
+__global__ void __launch_bounds__(SPL_BLOCK, 2) sel_split3_kernel(SelArgs a, int lo, int bits)
+{
+    using S = SplShape<C>;
+    constexpr int E = S::E, VEC = S::VEC;
+    constexpr bool HAS_V = !std::is_same<V, uint8_t>::value;
+    __shared__ uint32_t sh[SEL_BINS];
+    __shared__ uint32_t s_mask[SPL_SUB][SPL_WARPS][E][2];   // class L, class G
+    __shared__ uint32_t s_cnt[SPL_WARPS][3];
+    __shared__ uint32_t s_base[SPL_WARPS][3];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int nb = 1 << bits;
     for (int i = tid; i < nb; i += SPL_BLOCK) sh[i] = 0;
     __syncthreads();
     const Codec<C> cx(a.xf);
     const C pre = (C)a.st->prefix, msk = (C)a.st->mask;
-    const size_t b_lo = a.st->b_lo, b_hi = a.st->b_lo + a.st->b_n;
+    // positions and slots fit 32 bits: selects above XSS_RADIX_MAX_N keys sort
+    const uint32_t n = (uint32_t)a.n;
+    const uint32_t b_hi = (uint32_t)(a.st->b_lo + a.st->b_n);
     const C *keys = static_cast<const C *>(a.keys);
     const V *vals = static_cast<const V *>(a.vals);
-    C *mis_k = static_cast<C *>(a.mis_k);
-    V *mis_v = static_cast<V *>(a.mis_v);
+    C *scr_k = static_cast<C *>(a.mis_k);
+    V *scr_v = static_cast<V *>(a.mis_v);
     C *cand = static_cast<C *>(a.cand);
-    const size_t n = a.n;
+    uint32_t *cand_pos = static_cast<uint32_t *>(a.cand_p);
+    V *cand_val = static_cast<V *>(a.cand_p);
     const bool vec_ok = (reinterpret_cast<uintptr_t>(keys) & 15) == 0;
+    const bool vals_vec = HAS_V && vals != nullptr &&
+                          (reinterpret_cast<uintptr_t>(vals) % (VEC * sizeof(V))) == 0;
     const uint32_t lt = (1u << lane) - 1u, bit = 1u << lane;
-    const size_t rs[3] = {0, b_lo, b_hi};
-    // output q: 0 = list L, 1 = list G, 2 = candidates, 3 = holes of region 0,
-    // 4 = holes of region 2
-    auto outputs = [&](const uint32_t (&m)[4], uint32_t act, uint32_t (&o)[5]) {
-        o[0] = m[0] & ~m[2];
-        o[1] = m[1] & ~m[3];
-        o[2] = act & ~(m[0] | m[1]);
-        o[3] = m[2] & ~m[0];
-        o[4] = m[3] & ~m[1];
-    };
-    auto pos = [&](size_t w0, int e) {
-        return w0 + ((size_t)(e / VEC) * 32 + lane) * VEC + (e % VEC);
-    };
-    for (size_t s0 = (size_t)blockIdx.x * S::STEP; s0 < n; s0 += (size_t)gridDim.x * S::STEP) {
-        // ---- vote every sub-step; masks to shared memory, counts per warp
-        uint32_t tot[5] = {0, 0, 0, 0, 0};
+    const uint32_t lane0 = (uint32_t)lane * VEC;   // lane's first key in a vector row
+    for (uint32_t s0 = blockIdx.x * (uint32_t)S::STEP; s0 < n; s0 += gridDim.x * (uint32_t)S::STEP) {
+        uint32_t tL = 0, tG = 0, tC = 0;
         C raw[E], nxt[E];
-        spl_load<C>(keys, n, s0 + (size_t)warp * S::WSUB, lane, vec_ok, nxt);
+        spl_load<C>(keys, n, s0 + (uint32_t)warp * S::WSUB, lane, vec_ok, nxt);
 #pragma unroll 1
         for (int sub = 0; sub < SPL_SUB; ++sub) {
-            const size_t w0 = s0 + (size_t)sub * S::SUB + (size_t)warp * S::WSUB;
+            const uint32_t w0 = s0 + (uint32_t)sub * S::SUB + (uint32_t)warp * S::WSUB;
 #pragma unroll
             for (int e = 0; e < E; ++e) raw[e] = nxt[e];
             if (sub + 1 < SPL_SUB) spl_load<C>(keys, n, w0 + S::SUB, lane, vec_ok, nxt);
 #pragma unroll
             for (int e = 0; e < E; ++e) {
-                const size_t p = pos(w0, e);
+                const uint32_t p = w0 + (uint32_t)(e / VEC) * (32 * VEC) + lane0 + (e % VEC);
                 const bool in = p < n;
                 const C c = cx.to(raw[e]);
                 const C top = (C)(c & msk);
-                uint32_t m[4];
-                m[0] = __ballot_sync(0xffffffffu, in && top < pre);
-                m[1] = __ballot_sync(0xffffffffu, in && top > pre);
-                m[2] = __ballot_sync(0xffffffffu, in && p < b_lo);
-                m[3] = __ballot_sync(0xffffffffu, in && p >= b_hi);
-                const uint32_t act = __ballot_sync(0xffffffffu, in);
-                if (in && top == pre) atomicAdd(&sh[uint32_t(c >> lo) & (uint32_t)(nb - 1)], 1u);
-                if (a.op == SOP_ARG && in && (p < b_lo || p >= b_hi)) a.out_idx[p] = p;
-                if (lane < 4) s_mask[sub][warp][e][lane] = m[lane];
-                uint32_t o[5];
-                outputs(m, act, o);
-#pragma unroll
-                for (int q = 0; q < 5; ++q) tot[q] += __popc(o[q]);
+                const bool isL = in && top < pre, isG = in && top > pre;
+                const bool isC = in && !isL && !isG;
+                const uint32_t mL = __ballot_sync(0xffffffffu, isL);
+                const uint32_t mG = __ballot_sync(0xffffffffu, isG);
+                if (isC) atomicAdd(&sh[uint32_t(c >> lo) & (uint32_t)(nb - 1)], 1u);
+                if (lane == 0) s_mask[sub][warp][e][0] = mL;
+                if (lane == 1) s_mask[sub][warp][e][1] = mG;
+                tL += __popc(mL);
+                tG += __popc(mG);
+                tC += __popc(__ballot_sync(0xffffffffu, isC));
             }
         }
-        uint32_t mine = tot[0];
-#pragma unroll
-        for (int q = 1; q < 5; ++q)
-            if (lane == q) mine = tot[q];
-        if (lane < 5) s_cnt[warp][lane] = mine;
+        if (lane < 3) s_cnt[warp][lane] = lane == 0 ? tL : (lane == 1 ? tG : tC);
         __syncthreads();
-        // ---- one reservation per output for the CTA's step
-        if (tid < 5) {
+        if (tid < 3) {
             uint32_t sum = 0;
             for (int w = 0; w < SPL_WARPS; ++w) sum += s_cnt[w][tid];
-            unsigned long long b = 0;
+            uint32_t b = 0;
             if (sum) {
-                if (tid == 2) b = atomicAdd(&a.st->cand_n, (unsigned long long)sum);
-                else if (tid < 2) b = atomicAdd(&a.st->nmis[tid == 0 ? 0 : 2], sum);
-                else b = atomicAdd(&a.st->nhole[tid == 3 ? 0 : 2], sum);
+                if (tid == 2) b = (uint32_t)atomicAdd(&a.st->cand_n, (unsigned long long)sum);
+                else b = atomicAdd(&a.st->nmis[tid == 0 ? 0 : 2], sum);
             }
+            if (tid == 1) b += b_hi;
             for (int w = 0; w < SPL_WARPS; ++w) {
                 s_base[w][tid] = b;
                 b += s_cnt[w][tid];
             }
         }
         __syncthreads();
-        // ---- reload (L2) and write
-        unsigned long long run[5];
-#pragma unroll
-        for (int q = 0; q < 5; ++q) run[q] = s_base[warp][q];
+        uint32_t rL = s_base[warp][0], rG = s_base[warp][1], rC = s_base[warp][2];
 #pragma unroll 1
         for (int sub = 0; sub < SPL_SUB; ++sub) {
-            const size_t w0 = s0 + (size_t)sub * S::SUB + (size_t)warp * S::WSUB;
+            const uint32_t w0 = s0 + (uint32_t)sub * S::SUB + (uint32_t)warp * S::WSUB;
             if (w0 >= n) break;
             spl_load<C>(keys, n, w0, lane, vec_ok, raw);
+            V vv[E];
+            if constexpr (HAS_V)
+                if (a.op == SOP_KV) spl_load_vals<C, V>(vals, n, w0, lane, vals_vec, vv);
 #pragma unroll
             for (int e = 0; e < E; ++e) {
-                const size_t p = pos(w0, e);
+                const uint32_t p = w0 + (uint32_t)(e / VEC) * (32 * VEC) + lane0 + (e % VEC);
                 const uint32_t act = __ballot_sync(0xffffffffu, p < n);
-                uint32_t m[4];
-#pragma unroll
-                for (int i = 0; i < 4; ++i) m[i] = s_mask[sub][warp][e][i];
-                uint32_t o[5];
-                outputs(m, act, o);
-                if (o[2] & bit) {
-                    const unsigned long long at = run[2] + __popc(o[2] & lt);
-                    if (at < n) {
-                        cand[at] = cx.to(raw[e]);
-                        if (a.op == SOP_ARG) static_cast<uint32_t *>(a.cand_p)[at] = (uint32_t)p;
-                        else if constexpr (HAS_V)
-                            if (a.op == SOP_KV) static_cast<V *>(a.cand_p)[at] = vals[p];
-                    }
-                }
-#pragma unroll
-                for (int x = 0; x < 2; ++x) {
-                    if (o[x] & bit) {
-                        const unsigned long long at = rs[2 * x] + run[x] + __popc(o[x] & lt);
+                const uint32_t mL = s_mask[sub][warp][e][0], mG = s_mask[sub][warp][e][1];
+                const uint32_t mC = act & ~(mL | mG);
+                if (act & bit) {
+                    if (mL & bit) {
+                        const uint32_t at = rL + __popc(mL & lt);
+                        if (at >= n) {
+                        } else if (a.op == SOP_ARG) {
+                            a.out_idx[at] = p;
+                        } else {
+                            scr_k[at] = raw[e];
+                            if constexpr (HAS_V)
+                                if (a.op == SOP_KV) scr_v[at] = vv[e];
+                        }
+                    } else if (mG & bit) {
+                        const uint32_t at = rG + __popc(mG & lt);
                         if (at < n) {
                             if (a.op == SOP_ARG) {
-                                reinterpret_cast<uint32_t *>(a.mis_v)[at] = (uint32_t)p;
+                                a.out_idx[at] = p;
                             } else {
-                                mis_k[at] = raw[e];
+                                scr_k[at] = raw[e];
                                 if constexpr (HAS_V)
-                                    if (a.op == SOP_KV) mis_v[at] = vals[p];
+                                    if (a.op == SOP_KV) scr_v[at] = vv[e];
                             }
                         }
-                    }
-                    if (o[3 + x] & bit) {
-                        const unsigned long long at = rs[2 * x] + run[3 + x] + __popc(o[3 + x] & lt);
-                        if (at < n) a.holes[at] = (uint32_t)p;
+                    } else {
+                        const uint32_t at = rC + __popc(mC & lt);
+                        if (at < n) {
+                            cand[at] = cx.to(raw[e]);
+                            if (a.op == SOP_ARG) cand_pos[at] = p;
+                            else if constexpr (HAS_V)
+                                if (a.op == SOP_KV) cand_val[at] = vv[e];
+                        }
                     }
                 }
-#pragma unroll
-                for (int q = 0; q < 5; ++q) run[q] += __popc(o[q]);
+                rL += __popc(mL);
+                rG += __popc(mG);
+                rC += __popc(mC);
             }
         }
         __syncthreads();   // s_mask / s_cnt / s_base are rewritten by the next step
@@ -641,6 +784,46 @@ __global__ void __launch_bounds__(SPL_BLOCK, 2) sel_split_vote_kernel(SelArgs a,
     __syncthreads();
     for (int i = tid; i < nb; i += SPL_BLOCK)
         if (sh[i]) atomicAdd(&a.st->hist[i], sh[i]);
+}
+
+// The scratch regions [0, b_lo) and [b_hi, n) into the array (keys, and
+// values for key-value selects); four elements per thread in flight.
+template <typename C, typename V>
+__global__ void __launch_bounds__(256) sel_copyback_kernel(SelArgs a)
+{
+    constexpr bool HAS_V = !std::is_same<V, uint8_t>::value;
+    const size_t b_lo = a.st->b_lo, b_hi = a.st->b_lo + a.st->b_n, n = a.n;
+    const size_t m = b_lo + (n - min(b_hi, n));      // elements to move
+    C *keys = static_cast<C *>(a.keys);
+    V *vals = static_cast<V *>(a.vals);
+    const C *scr_k = static_cast<const C *>(a.mis_k);
+    const V *scr_v = static_cast<const V *>(a.mis_v);
+    const size_t stride = (size_t)gridDim.x * 256;
+    constexpr int U = 4;
+    for (size_t j0 = (size_t)blockIdx.x * 256 + threadIdx.x; j0 < m; j0 += U * stride) {
+        C k[U];
+        V v[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const size_t j = j0 + u * stride;
+            const size_t i = j < b_lo ? j : b_hi + (j - b_lo);
+            if (j < m) {
+                k[u] = scr_k[i];
+                if constexpr (HAS_V)
+                    if (a.op == SOP_KV) v[u] = scr_v[i];
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const size_t j = j0 + u * stride;
+            const size_t i = j < b_lo ? j : b_hi + (j - b_lo);
+            if (j < m) {
+                keys[i] = k[u];
+                if constexpr (HAS_V)
+                    if (a.op == SOP_KV) vals[i] = v[u];
+            }
+        }
+    }
 }
 
 // B's region rewritten from the candidates, partitioned around K:
@@ -839,18 +1022,34 @@ static int select_launch(int op, KeyXform xf, void *keys, void *vals, uint64_t *
     }
     const int W = 8 * (int)sizeof(C);
     const int rounds = (W + SEL_DIGIT - 1) / SEL_DIGIT;   // 3 (32-bit) or 6 (64-bit)
+    // Where k is not near either end, a good share of the keys on each side
+    // of the bucket lie in the other side's region: writing every key once to
+    // a scratch copy (and copying its outer regions back) costs less than
+    // listing and moving the misplaced ones (qselect float32 2^27, k = 2^26:
+    // 0.76 against 1.38 ms).  Within n / 4096 of an end only a few keys are
+    // recorded, and the sparse in-place split reads the array at little more
+    // than memory speed.
+    const bool out_of_place = std::min(k, n - 1 - k) >= n / 4096;
     for (int r = 0; r < rounds; ++r) {
         const int hi = W - SEL_DIGIT * r;
         const int lo = std::max(0, hi - SEL_DIGIT);
         const int bits = hi - lo;
-        if (r == 1) {
-            // one read of every key: candidates, their next-digit histogram,
-            // and the L / G lists and holes
+        if (r == 1 && out_of_place) {
+            // one read of every key: candidates and their next-digit
+            // histogram; L and G keys to the scratch copy's front and back
             const int sg = (int)std::max<size_t>(
                 1, std::min<size_t>((n + SplShape<C>::STEP - 1) / SplShape<C>::STEP,
                                     (size_t)sms * 4));
             XSS_LAUNCH(PK_SEL_COLLECT, s,
-                       (sel_split_vote_kernel<C, V><<<sg, SPL_BLOCK, 0, s>>>(a, lo, bits)));
+                       (sel_split3_kernel<C, V><<<sg, SPL_BLOCK, 0, s>>>(a, lo, bits)));
+        } else if (r == 1) {
+            // one read of every key: candidates, their next-digit histogram,
+            // and the lists and holes of the few misplaced L / G keys
+            const int sg = (int)std::max<size_t>(
+                1, std::min<size_t>((n + 8 * SplShape<C>::WSUB - 1) / (8 * SplShape<C>::WSUB),
+                                    (size_t)sms * 8));
+            XSS_LAUNCH(PK_SEL_COLLECT, s,
+                       (sel_split_sparse_kernel<C, V><<<sg, 256, 0, s>>>(a, lo, bits)));
         } else {
             // round 0 reads every key; later rounds only the candidates
             const int g = r >= 2 ? std::max(1, grid / 4) : grid;
@@ -864,8 +1063,16 @@ static int select_launch(int op, KeyXform xf, void *keys, void *vals, uint64_t *
     }
     XSS_LAUNCH(PK_SEL_PLACE, s, (sel_bpart_kernel<C, V><<<grid, 256, 0, s>>>(a)));
     XSS_CUDA_TRY(cudaGetLastError());
-    XSS_LAUNCH(PK_SEL_PLACE, s, (sel_place_kernel<C, V><<<grid, 256, 0, s>>>(a, 0)));
-    XSS_CUDA_TRY(cudaGetLastError());
+    if (out_of_place) {
+        if (op != SOP_ARG) {
+            XSS_LAUNCH(PK_SEL_PLACE, s,
+                       (sel_copyback_kernel<C, V><<<sms * 8, 256, 0, s>>>(a)));
+            XSS_CUDA_TRY(cudaGetLastError());
+        }
+    } else {
+        XSS_LAUNCH(PK_SEL_PLACE, s, (sel_place_kernel<C, V><<<grid, 256, 0, s>>>(a, 0)));
+        XSS_CUDA_TRY(cudaGetLastError());
+    }
     return XSS_OK;
 }
 

@@ -15,8 +15,11 @@
 
 // K32 (ranks packed two per register): 320,20,3,8,2,1,0 3.598 ms; 320,24,3,8,2,1,0 3.372 ms; 320,28,2,8,2,1,0 3.738 ms;
 // 320,32,2,8,2,1,0 3.513 ms; 320,40,2,8,2,1,0 5.198 ms; 384,32,2,8,2,1,0 3.323 ms; 256,40,2,8,2,1,0 3.788 ms; 256,32,3,8,2,1,0 4.101 ms
+// K32 pipelined form (PERSIST 3, resident CTAs holding two tiles), A/B against
+// 384,32,2,8,2,1,0 at 2^28: float32 3.586 vs 3.700 ms, uint32 3.293 vs 3.356 ms;
+// 384,32,2,8,2,3,0 3.704 / 3.390; 320,20,3,8,2,3,0 3.874 / 3.585; 256,28,3,8,2,3,0 3.671 / 3.372
 #ifndef XSS_CFG_K32
-#define XSS_CFG_K32 384, 32, 2, 8, 2, 1, 0
+#define XSS_CFG_K32 384, 28, 2, 8, 2, 3, 0
 #endif
 
 // K64: 512,16,1,16,2,1,1 10.686 ms; 512,20,1,16,2,1,1 9.931 ms; 512,24,1,16,2,1,1 9.505 ms; 768,16,1,16,2,1,1 10.688 ms
