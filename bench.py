@@ -201,6 +201,12 @@ class KeyValueSort(Workload):
     def host_run(self):
         self.xss.keyvalue_qsort(self.hk, self.hv)
 
+    def host_check(self):
+        # sorted keys, and every value (the original index) carries its key
+        idx = np.random.default_rng(5).integers(0, self.n, 1 << 16)
+        return bool((self.hk[1:] >= self.hk[:-1]).all()) and \
+            bool((self.hk0[self.hv[idx].astype(np.int64)] == self.hk[idx]).all())
+
     def host_bytes(self):
         return self.n * (self.kb + self.vb), self.n * (self.kb + self.vb)
 
@@ -273,6 +279,9 @@ class QsortF32(Workload):
 
     def host_run(self):
         self.xss.qsort(self.hk)
+
+    def host_check(self):
+        return bool((self.hk[1:] >= self.hk[:-1]).all())
 
     def host_bytes(self):
         return self.n * 4, self.n * 4
@@ -528,12 +537,21 @@ class ArgsortWorkload(Workload):
     def host_setup(self):
         self.hk = self.pinned(self.n * 8, np.dtype(self.kdt))
         self.hk[:] = self.k0.cpu().numpy()
+        # the indices go to the caller's pinned array (the reference's
+        # argsort(T*, size_t* arg, ...) form)
+        self.harg = self.pinned(self.n * 8, np.uint64)
 
     def host_restore(self):
         pass
 
     def host_run(self):
-        self.harg = self.xss.argsort(self.hk, self.desc, self.desc)
+        self.xss.argsort(self.hk, self.desc, self.desc, out=self.harg)
+
+    def host_check(self):
+        # the gathered keys are in order (NaN-free sample positions)
+        g = self.hk[self.harg[: 1 << 20].astype(np.int64)]
+        g = g[~np.isnan(g)] if g.dtype.kind == "f" else g
+        return bool((g[1:] <= g[:-1]).all()) if self.desc else bool((g[1:] >= g[:-1]).all())
 
     def host_bytes(self):
         return self.n * self.kb, self.n * 8
@@ -895,12 +913,13 @@ class ArgselectF32(SelectWorkload):
     def host_setup(self):
         self.hk = self.pinned(self.n * 4, np.float32)
         np.copyto(self.hk, self.k0.cpu().numpy())
+        self.harg = self.pinned(self.n * 8, np.uint64)   # the caller's index array
 
     def host_restore(self):
         pass
 
     def host_run(self):
-        self.xss.argselect(self.hk, self.k)
+        self.xss.argselect(self.hk, self.k, out=self.harg)
 
     def host_bytes(self):
         return self.n * 4, self.n * 8
@@ -1601,6 +1620,8 @@ def measure(args, ctx, workload, n_override, steps, warmup, do_e2e=True, do_cpu=
         bi, bo = wl.host_bytes()
         e2e = {"value": n * steps / t / 1e9, "unit": "Gkeys/s", "h2d_bytes_per_step": bi,
                "d2h_bytes_per_step": bo, "ms_per_step": t / steps * 1e3}
+        if hasattr(wl, "host_check"):
+            e2e["checked"] = bool(wl.host_check())   # the last step's host result
 
     cpu = None
     if rank == 0 and world == 1 and do_cpu:

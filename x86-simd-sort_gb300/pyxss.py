@@ -159,15 +159,23 @@ def partial_qsort(arr: np.ndarray, k: int, hasnan: bool = False,
                                   int(descending)), "partial_qsort")
 
 
-def argsort(arr: np.ndarray, hasnan: bool = False, descending: bool = False) -> np.ndarray:
-    out = np.empty(arr.size, dtype=np.uint64)
+def argsort(arr: np.ndarray, hasnan: bool = False, descending: bool = False,
+            out: np.ndarray = None) -> np.ndarray:
+    """Indices that sort arr; into `out` (uint64, arr.size) when given, as the
+    reference's argsort(T*, size_t* arg, ...) writes into the caller's array."""
+    if out is None:
+        out = np.empty(arr.size, dtype=np.uint64)
+    assert out.dtype == np.uint64 and out.size == arr.size
     check(lib().xss_argsort(dtype_id(arr.dtype), _ptr(arr), _ptr(out), arr.size, int(hasnan),
                             int(descending)), "argsort")
     return out
 
 
-def argselect(arr: np.ndarray, k: int, hasnan: bool = False) -> np.ndarray:
-    out = np.empty(arr.size, dtype=np.uint64)
+def argselect(arr: np.ndarray, k: int, hasnan: bool = False,
+              out: np.ndarray = None) -> np.ndarray:
+    if out is None:
+        out = np.empty(arr.size, dtype=np.uint64)
+    assert out.dtype == np.uint64 and out.size == arr.size
     check(lib().xss_argselect(dtype_id(arr.dtype), _ptr(arr), _ptr(out), k, arr.size,
                               int(hasnan)), "argselect")
     return out
