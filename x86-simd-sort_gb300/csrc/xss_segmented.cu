@@ -294,12 +294,15 @@ struct SegPlan {
 // lines measured for that form (two CTAs per SM) instead of the resident
 // lines tuned for one whole array.  Ranking by the count atomic (RANK 2) and
 // larger tiles took the 200,000-segment batch (4.2e9 keys) from 123.3 to
-// 93.5 ms (int32 -> uint32) and from 127.7 to 99.4 ms (float32).
+// 93.5 ms (int32 -> uint32) and from 127.7 to 99.4 ms (float32); three CTAs
+// per SM of 384 x 12 then to 89.5 / 94.6 ms (512 x 12 x 2: 93.9 / 99.7;
+// 256 x 12 x 4: 93.1 / 98.9; 256 x 16 x 3: 96.4 / 102.9; 512 x 8 x 3:
+// 97.9 / 100.7 ms).
 #ifndef XSS_SEGCFG_KEYS
 #define XSS_SEGCFG_KEYS 512, 16, 2, 16, 2, 0, 0
 #endif
 #ifndef XSS_SEGCFG_K32V32
-#define XSS_SEGCFG_K32V32 512, 12, 2, 16, 2, 0, 0
+#define XSS_SEGCFG_K32V32 384, 12, 3, 16, 2, 0, 0
 #endif
 #ifndef XSS_SEGCFG_DEFAULT
 #define XSS_SEGCFG_DEFAULT 256, 16, 2, 16, 2, 0, 0

@@ -497,6 +497,26 @@ __device__ __forceinline__ void spl_load(const C *keys, uint32_t n, uint32_t w0,
 // layout as the tag split above (lists and holes start at their region's
 // first position); argselect writes the identity of every position outside
 // B's region.
+// Identity positions of a full row (every lane's VEC consecutive keys) into
+// the index output, 16 bytes per store where the output is 16-byte aligned.
+template <typename C>
+__device__ __forceinline__ void spl_iota(uint64_t *out, uint32_t w0, uint32_t lane0, bool vec)
+{
+    using S = SplShape<C>;
+#pragma unroll
+    for (int v = 0; v < S::VECS; ++v) {
+        const uint32_t p = w0 + (uint32_t)v * (32 * S::VEC) + lane0;
+        if (vec) {
+#pragma unroll
+            for (int i = 0; i < S::VEC; i += 2)
+                *reinterpret_cast<ulonglong2 *>(out + p + i) = make_ulonglong2(p + i, p + i + 1);
+        } else {
+#pragma unroll
+            for (int i = 0; i < S::VEC; ++i) out[p + i] = p + i;
+        }
+    }
+}
+
 template <typename C, typename V>
 __global__ void __launch_bounds__(256) sel_split_sparse_kernel(SelArgs a, int lo, int bits)
 {
@@ -522,10 +542,28 @@ __global__ void __launch_bounds__(256) sel_split_sparse_kernel(SelArgs a, int lo
     const uint32_t lt = (1u << lane) - 1u, bit = 1u << lane;
     const uint32_t lane0 = (uint32_t)lane * VEC;
     const uint32_t wstride = gridDim.x * 8u * (uint32_t)S::WSUB;
+    const bool idx_vec = (reinterpret_cast<uintptr_t>(a.out_idx) & 15) == 0;
     for (uint32_t w0 = (blockIdx.x * 8u + (uint32_t)(tid >> 5)) * (uint32_t)S::WSUB; w0 < n;
          w0 += wstride) {
         C raw[E];
         spl_load<C>(keys, n, w0, lane, vec_ok, raw);
+        const uint32_t wend = w0 + (uint32_t)S::WSUB;     // the warp's keys: [w0, wend)
+        if (w0 >= b_hi && wend <= n) {
+            // the whole row lies in region 2 (the common case for k near 0):
+            // a key needs recording only if it is not of class G
+            bool any2 = false;
+#pragma unroll
+            for (int e = 0; e < E; ++e) any2 |= (C)(cx.to(raw[e]) & msk) <= pre;
+            if (a.op == SOP_ARG) spl_iota<C>(a.out_idx, w0, lane0, idx_vec);
+            if (!__any_sync(0xffffffffu, any2)) continue;
+        } else if (wend <= b_lo) {
+            // the whole row lies in region 0 (k near n - 1): record non-L keys
+            bool any0 = false;
+#pragma unroll
+            for (int e = 0; e < E; ++e) any0 |= (C)(cx.to(raw[e]) & msk) >= pre;
+            if (a.op == SOP_ARG) spl_iota<C>(a.out_idx, w0, lane0, idx_vec);
+            if (!__any_sync(0xffffffffu, any0)) continue;
+        }
         uint32_t cls4 = 0, reg4 = 0;   // 2 bits per key slot
         bool any = false;
 #pragma unroll
@@ -692,22 +730,23 @@ __global__ void __launch_bounds__(SPL_BLOCK, 2) sel_split3_kernel(SelArgs a, int
 #pragma unroll
             for (int e = 0; e < E; ++e) raw[e] = nxt[e];
             if (sub + 1 < SPL_SUB) spl_load<C>(keys, n, w0 + S::SUB, lane, vec_ok, nxt);
+            const bool full = w0 + (uint32_t)S::WSUB <= n;   // uniform across the warp
 #pragma unroll
             for (int e = 0; e < E; ++e) {
                 const uint32_t p = w0 + (uint32_t)(e / VEC) * (32 * VEC) + lane0 + (e % VEC);
-                const bool in = p < n;
+                const bool in = full || p < n;
                 const C c = cx.to(raw[e]);
                 const C top = (C)(c & msk);
                 const bool isL = in && top < pre, isG = in && top > pre;
-                const bool isC = in && !isL && !isG;
                 const uint32_t mL = __ballot_sync(0xffffffffu, isL);
                 const uint32_t mG = __ballot_sync(0xffffffffu, isG);
-                if (isC) atomicAdd(&sh[uint32_t(c >> lo) & (uint32_t)(nb - 1)], 1u);
+                if (in && !isL && !isG) atomicAdd(&sh[uint32_t(c >> lo) & (uint32_t)(nb - 1)], 1u);
                 if (lane == 0) s_mask[sub][warp][e][0] = mL;
                 if (lane == 1) s_mask[sub][warp][e][1] = mG;
                 tL += __popc(mL);
                 tG += __popc(mG);
-                tC += __popc(__ballot_sync(0xffffffffu, isC));
+                tC += full ? 32u - __popc(mL | mG)
+                           : __popc(__ballot_sync(0xffffffffu, in) & ~(mL | mG));
             }
         }
         if (lane < 3) s_cnt[warp][lane] = lane == 0 ? tL : (lane == 1 ? tG : tC);
@@ -736,47 +775,35 @@ __global__ void __launch_bounds__(SPL_BLOCK, 2) sel_split3_kernel(SelArgs a, int
             V vv[E];
             if constexpr (HAS_V)
                 if (a.op == SOP_KV) spl_load_vals<C, V>(vals, n, w0, lane, vals_vec, vv);
+            const bool full = w0 + (uint32_t)S::WSUB <= n;   // uniform across the warp
 #pragma unroll
             for (int e = 0; e < E; ++e) {
                 const uint32_t p = w0 + (uint32_t)(e / VEC) * (32 * VEC) + lane0 + (e % VEC);
-                const uint32_t act = __ballot_sync(0xffffffffu, p < n);
+                const uint32_t act = full ? 0xffffffffu : __ballot_sync(0xffffffffu, p < n);
                 const uint32_t mL = s_mask[sub][warp][e][0], mG = s_mask[sub][warp][e][1];
                 const uint32_t mC = act & ~(mL | mG);
-                if (act & bit) {
-                    if (mL & bit) {
-                        const uint32_t at = rL + __popc(mL & lt);
-                        if (at >= n) {
-                        } else if (a.op == SOP_ARG) {
-                            a.out_idx[at] = p;
-                        } else {
-                            scr_k[at] = raw[e];
-                            if constexpr (HAS_V)
-                                if (a.op == SOP_KV) scr_v[at] = vv[e];
-                        }
-                    } else if (mG & bit) {
-                        const uint32_t at = rG + __popc(mG & lt);
-                        if (at < n) {
-                            if (a.op == SOP_ARG) {
-                                a.out_idx[at] = p;
-                            } else {
-                                scr_k[at] = raw[e];
-                                if constexpr (HAS_V)
-                                    if (a.op == SOP_KV) scr_v[at] = vv[e];
-                            }
-                        }
+                // this key's class mask and slot; one store path per output kind
+                const bool inL = mL & bit, inG = mG & bit;
+                const uint32_t m = inL ? mL : (inG ? mG : mC);
+                const uint32_t at = (inL ? rL : (inG ? rG : rC)) + __popc(m & lt);
+                if ((act & bit) && at < n) {
+                    if (!inL && !inG) {
+                        cand[at] = cx.to(raw[e]);
+                        if (a.op == SOP_ARG) cand_pos[at] = p;
+                        else if constexpr (HAS_V)
+                            if (a.op == SOP_KV) cand_val[at] = vv[e];
+                    } else if (a.op == SOP_ARG) {
+                        a.out_idx[at] = p;
                     } else {
-                        const uint32_t at = rC + __popc(mC & lt);
-                        if (at < n) {
-                            cand[at] = cx.to(raw[e]);
-                            if (a.op == SOP_ARG) cand_pos[at] = p;
-                            else if constexpr (HAS_V)
-                                if (a.op == SOP_KV) cand_val[at] = vv[e];
-                        }
+                        scr_k[at] = raw[e];
+                        if constexpr (HAS_V)
+                            if (a.op == SOP_KV) scr_v[at] = vv[e];
                     }
                 }
-                rL += __popc(mL);
-                rG += __popc(mG);
-                rC += __popc(mC);
+                const uint32_t nL = __popc(mL), nG = __popc(mG);
+                rL += nL;
+                rG += nG;
+                rC += full ? 32u - nL - nG : __popc(mC);
             }
         }
         __syncthreads();   // s_mask / s_cnt / s_base are rewritten by the next step
