@@ -263,9 +263,9 @@ __global__ void __launch_bounds__(BLOCK, MINB) seg_pass_kernel(SegArgs a, int pa
                       a.seg_start + ((size_t)l * a.passes + pass) * RADIX,
                       a.status + (size_t)(pass & 1) * a.T * RADIX};
     const Codec<C> cx(a.xf);   // unused with ROLE_RUNTIME (from_code decides)
-    pass_tile<C, V, BLOCK, ITEMS, LB, RANK, DPT, ROLE_RUNTIME>(ra, pd, pass, job, key, val, s_k,
-                                                               s_v, ps, kdst, vdst, cx,
-                                                               NoAfterRank{});
+    // s_dyn holds TILE keys then TILE values: the layout pair staging needs
+    pass_tile<C, V, BLOCK, ITEMS, LB, RANK, DPT, ROLE_RUNTIME, pair_staged<C, VS, RANK>()>(
+        ra, pd, pass, job, key, val, s_k, s_v, ps, kdst, vdst, cx, NoAfterRank{});
 }
 
 // ---------------------------------------------------------------------------

@@ -18,6 +18,10 @@
 // K32 pipelined form (PERSIST 3, resident CTAs holding two tiles), A/B against
 // 384,32,2,8,2,1,0 at 2^28: float32 3.586 vs 3.700 ms, uint32 3.293 vs 3.356 ms;
 // 384,32,2,8,2,3,0 3.704 / 3.390; 320,20,3,8,2,3,0 3.874 / 3.585; 256,28,3,8,2,3,0 3.671 / 3.372
+// One larger CTA per SM (longer tiles, fewer on the look-back chain), float32 / uint32 against
+// 3.588 / 3.294: 768,28,1,8,2,3,0 3.807 / 3.520; 768,24,1,8,2,3,0 3.889 / 3.601;
+// 640,32,1,8,2,3,0 3.911 / 3.629; 512,40,1,8,2,3,0 4.035 / 3.760; 512,32,1,8,2,3,0 4.222 / 3.946;
+// 768,28,1,16,2,3,0 3.883 / 3.606 (two CTAs per SM overlap each other's barrier phases)
 #ifndef XSS_CFG_K32
 #define XSS_CFG_K32 384, 28, 2, 8, 2, 3, 0
 #endif
