@@ -159,8 +159,10 @@ int xss_gpu_keyvalue_partial_sort(int key_dtype, int val_dtype, void *d_keys,
  * that device every kernel a call can launch (CUDA loads kernel code lazily,
  * and that load does allocate device memory), by sorting small arrays inside
  * the array itself.  Make that first call once per device, outside the code
- * that must not allocate, and before any stream capture; every later call on
- * the device allocates nothing.  All calls share the one array and find the
+ * that must not allocate; every later call on the device allocates nothing.
+ * No call can be made while its stream is being captured (into a CUDA graph):
+ * each one copies its status word to the host and synchronises the stream.
+ * All calls share the one array and find the
  * previous call's data in it: calls whose GPU work could overlap (other
  * streams, other host threads) race on it and must be serialised by the caller.
  */

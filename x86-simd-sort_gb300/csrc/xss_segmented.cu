@@ -297,7 +297,15 @@ struct SegPlan {
 // 93.5 ms (int32 -> uint32) and from 127.7 to 99.4 ms (float32); three CTAs
 // per SM of 384 x 12 then to 89.5 / 94.6 ms (512 x 12 x 2: 93.9 / 99.7;
 // 256 x 12 x 4: 93.1 / 98.9; 256 x 16 x 3: 96.4 / 102.9; 512 x 8 x 3:
-// 97.9 / 100.7 ms).
+// 97.9 / 100.7 ms).  A resident form (CTAs claiming tiles in order, the next
+// tile claimed once the current one is ranked and bulk-copied when it is
+// full and 16-byte aligned) measured slower on the literal batch: 99.5 ms
+// (512 x 10, 2 CTAs per SM), 105.9 (256 x 14 x 3), 107.0 (384 x 12 x 2),
+// 120.0 (512 x 24 x 1) against 89.4 ms, and 1.6 s with 4 CTAs per SM of
+// 256 x 10.  Only segments whose first key sits on a 16-byte boundary can be
+// bulk-copied, the second buffer costs a CTA per SM, and a tile claimed
+// ahead publishes its counts a tile later, so its successors' look-backs
+// poll longer (with many small tiles in flight the polling fills L2).
 #ifndef XSS_SEGCFG_KEYS
 #define XSS_SEGCFG_KEYS 512, 16, 2, 16, 2, 0, 0
 #endif
