@@ -3,6 +3,10 @@ overlapped with chunk sorts, then merged and copied back slice by slice).
 Its results must equal the device-pointer sort of the same input exactly
 (both are stable where order can be told apart), from pageable and from
 pinned host buffers."""
+import os
+import subprocess
+import sys
+
 import numpy as np
 import pytest
 
@@ -10,6 +14,7 @@ from golden_io import DT
 from xss_arrays import assert_same_sorted, bit_code, get_array
 
 pytestmark = pytest.mark.gpu
+HERE = os.path.dirname(os.path.abspath(__file__))
 
 N = (1 << 22) + 12345
 
@@ -59,3 +64,14 @@ def test_argsort_host_pipeline_is_stable_order(xss, cuda, dtype):
     arg = xss.argsort(x, True, True)
     want = np.argsort(bit_code(x, True), kind="stable")
     assert np.array_equal(arg.astype(np.int64), want)
+
+
+@pytest.mark.parametrize("chunk", ["899840", "649984", "499968"])
+def test_host_pipeline_more_chunks(xss, cuda, chunk):
+    # 5, 7 and 9 chunks: merge levels run between the chunk sorts and meet
+    # partial blocks (a child process, as the chunk length is read once)
+    env = dict(os.environ, XSS_MERGE_CHUNK=chunk)
+    r = subprocess.run([sys.executable, os.path.join(HERE, "host_pipeline_cases.py")], env=env,
+                       stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True, timeout=900)
+    assert r.returncode == 0, r.stdout[-4000:]
+    assert "0 failures" in r.stdout

@@ -350,15 +350,27 @@ int big_sort(int op, int kbytes, KeyXform xf, void *keys, void *vals, int vbytes
 
 // ---------------------------------------------------------------------------
 // Host-pointer sorts of large arrays, pipelined: the array is cut into
-// PIPE_CHUNKS chunks; each chunk's host-to-device copy runs on its own stream
-// while the previous chunks are already being radix-sorted, the sorted runs are
-// merged, and the last merge runs in PIPE_SLICES output slices, each copied
+// chunks; each chunk's host-to-device copy runs on its own stream while the
+// previous chunks are already being radix-sorted, the sorted runs are merged
+// as soon as both halves of a merge are sorted, and the last merge runs in
+// PIPE_SLICES output slices, each copied
 // back to the host as soon as it is written.  The copies in and out (the host
 // link) then bound the call instead of copy-in + sort + copy-out.  Chunk sorts
 // and the merge are stable, so results equal the one-piece sort's.  Pinned
 // host buffers make every copy asynchronous; pageable ones are staged by the
 // driver chunk by chunk, which still overlaps the chunk sorts.
+// Chunks: PIPE_CHUNKS_LARGE from PIPE_LARGE_N keys on, else PIPE_CHUNKS (the
+// chunks of a smaller array stay long enough for the large-array pass lines).
+// Measured on 2^28 int64 -> uint64 pairs from pinned buffers (median of 12
+// calls, all variants in one process): 49.65 ms with every merge level after
+// the last chunk sort, 48.52 with the levels between the chunk sorts, 48.24
+// with 6 chunks, 47.73 with 8.
+#ifndef XSS_PIPE_CHUNKS_LARGE
+#define XSS_PIPE_CHUNKS_LARGE 8
+#endif
 constexpr int PIPE_CHUNKS = 4;
+constexpr int PIPE_CHUNKS_LARGE = XSS_PIPE_CHUNKS_LARGE;
+constexpr size_t PIPE_LARGE_N = size_t(1) << 27;
 constexpr int PIPE_SLICES = 8;
 
 struct PipeCtx {
@@ -406,7 +418,8 @@ static int pipelined_sort_c(int op, KeyXform xf, C *hk, V *hv, uint64_t *hidx, s
     constexpr size_t VB = HAS_V ? sizeof(V) : 0;
     const int kb = sizeof(C);
     const int sop = op == SOP_ARG ? SOP_KV : op;         // argsort sorts (key, position)
-    size_t chunk = align_up((n + PIPE_CHUNKS - 1) / PIPE_CHUNKS, 256);
+    const size_t parts = n >= PIPE_LARGE_N ? PIPE_CHUNKS_LARGE : PIPE_CHUNKS;
+    size_t chunk = align_up((n + parts - 1) / parts, 256);
     chunk = std::min(chunk, merge_chunk());
     const size_t nch = (n + chunk - 1) / chunk;
     if (nch > 64) return XSS_ETOOBIG;
@@ -436,6 +449,34 @@ static int pipelined_sort_c(int op, KeyXform xf, C *hk, V *hv, uint64_t *hidx, s
             XSS_CUDA_TRY(cudaGetLastError());
         }
     }
+    // Merge levels: level l (1..L) merges pairs of level l-1 runs of chunk << (l-1)
+    // keys; level l's runs live in buffer l % 2 (level 0: the sorted chunks, in
+    // buffer 0).  Every level below L merges a block as soon as the chunks under
+    // it are sorted, between the chunk sorts, so the merges overlap the copies
+    // of later chunks; level L runs in slices, each copied out once written.
+    const KeyXform mxf{xf.kind, xf.desc, 0};   // the chunk sorts wrote canonical NaNs
+    int L = 0;
+    while ((chunk << L) < n) ++L;
+    C *const bk[2] = {dk, dk1};
+    V *const bv[2] = {dv, dv1};
+    auto merge_block = [&](int l, size_t j) -> int {
+        const size_t run = chunk << (l - 1), b = j * 2 * run;
+        if (b >= n) return XSS_OK;
+        const size_t na = std::min(run, n - b), nb = std::min(run, n - b - na);
+        C *const sk = bk[(l - 1) & 1], *const tk = bk[l & 1];
+        V *const sv = bv[(l - 1) & 1], *const tv = bv[l & 1];
+        if (nb == 0) {
+            XSS_CUDA_TRY(cudaMemcpyAsync(tk + b, sk + b, na * kb, cudaMemcpyDeviceToDevice,
+                                         c->s_cmp));
+            if constexpr (HAS_V)
+                XSS_CUDA_TRY(cudaMemcpyAsync(tv + b, sv + b, na * VB, cudaMemcpyDeviceToDevice,
+                                             c->s_cmp));
+            return XSS_OK;
+        }
+        return merge_pass<C, V>(sk + b, sk + b + na, HAS_V ? sv + b : nullptr,
+                                HAS_V ? sv + b + na : nullptr, na, nb, tk + b,
+                                HAS_V ? tv + b : nullptr, split, mxf, c->s_cmp);
+    };
     for (size_t i = 0; i < nch; ++i) {
         const size_t b = i * chunk, len = std::min(chunk, n - b);
         touch_host_pages(hk + b, len * kb);
@@ -451,31 +492,22 @@ static int pipelined_sort_c(int op, KeyXform xf, C *hk, V *hv, uint64_t *hidx, s
         rc = radix_sort_chunk(sop, kb, xf, dk + b, HAS_V ? (void *)(dv + b) : nullptr, (int)VB,
                               nullptr, len, base + o_w, cws_bytes, c->s_cmp);
         if (rc) return rc;
-    }
-    const KeyXform mxf{xf.kind, xf.desc, 0};   // the chunk sorts wrote canonical NaNs
-    // every merge level but the last
-    C *sk = dk, *tk = dk1;
-    V *sv = dv, *tv = dv1;
-    size_t run = chunk;
-    for (; 2 * run < n; run *= 2) {
-        for (size_t b = 0; b < n; b += 2 * run) {
-            const size_t na = std::min(run, n - b), nb = std::min(run, n - b - na);
-            if (nb == 0) {
-                XSS_CUDA_TRY(cudaMemcpyAsync(tk + b, sk + b, na * kb, cudaMemcpyDeviceToDevice,
-                                             c->s_cmp));
-                if constexpr (HAS_V)
-                    XSS_CUDA_TRY(cudaMemcpyAsync(tv + b, sv + b, na * VB,
-                                                 cudaMemcpyDeviceToDevice, c->s_cmp));
-                continue;
+        // the level-l blocks this chunk completes (after the last chunk: every
+        // remaining, possibly partial, block); a block's halves were written
+        // by the lower levels just before it, on the same stream
+        for (int l = 1; l < L; ++l) {
+            const size_t per_block = size_t(1) << l;   // chunks under a level-l block
+            if ((i + 1) % per_block == 0 || i == nch - 1) {
+                rc = merge_block(l, i / per_block);
+                if (rc) return rc;
             }
-            rc = merge_pass<C, V>(sk + b, sk + b + na, HAS_V ? sv + b : nullptr,
-                                  HAS_V ? sv + b + na : nullptr, na, nb, tk + b,
-                                  HAS_V ? tv + b : nullptr, split, mxf, c->s_cmp);
-            if (rc) return rc;
         }
-        std::swap(sk, tk);
-        std::swap(sv, tv);
     }
+    // level L's input (with one chunk: the sorted chunk itself) and output
+    const int li = L > 0 ? (L - 1) & 1 : 0;
+    C *const sk = bk[li], *const tk = bk[L & 1];
+    V *const sv = bv[li], *const tv = bv[L & 1];
+    const size_t run = L > 0 ? chunk << (L - 1) : n;
     // the last level in slices, each copied out once written
     C *ok = sk;
     V *ov = sv;
