@@ -93,7 +93,9 @@ __device__ __forceinline__ uint32_t sel_block_excl_scan(uint32_t v, uint32_t *s_
 // One histogram round over every key (round 0) or over the compacted
 // candidates (rounds >= 2; round 1 is the split pass).  16-byte vector
 // loads, four per thread in flight, keep enough bytes moving to cover memory
-// latency; an unaligned array takes the scalar loop.
+// latency; an unaligned array takes the scalar loop.  (Issuing each step's
+// loads before the previous step's keys are counted, and interleaved copies
+// of the bins, measured no faster.)
 template <typename C>
 __global__ void __launch_bounds__(256) sel_hist_kernel(SelArgs a, int round, int lo, int bits,
                                                        int from_keys)
@@ -813,42 +815,56 @@ __global__ void __launch_bounds__(SPL_BLOCK, 2) sel_split3_kernel(SelArgs a, int
         if (sh[i]) atomicAdd(&a.st->hist[i], sh[i]);
 }
 
+// dst[i] = src[i] for i in [s, e) by every thread of the grid (global thread
+// gtid of `stride`): 16-byte vectors, four per thread in flight, over the part
+// of the range that starts on a 16-byte boundary in both arrays; single
+// elements before and after it, and everywhere if the arrays' alignments differ.
+template <typename T>
+__device__ __forceinline__ void copy_range(T *dst, const T *src, size_t s, size_t e, size_t gtid,
+                                           size_t stride)
+{
+    constexpr size_t VW = 16 / sizeof(T);
+    constexpr int U = 4;
+    if (s >= e) return;
+    const bool al = ((reinterpret_cast<uintptr_t>(dst) | reinterpret_cast<uintptr_t>(src)) & 15) == 0;
+    const size_t a0 = al ? std::min(e, (s + VW - 1) / VW * VW) : e;   // first vector element
+    const size_t a1 = al ? std::max(a0, e / VW * VW) : e;             // end of the vectors
+    for (size_t i = s + gtid; i < a0; i += stride) dst[i] = src[i];
+    for (size_t i = a1 + gtid; i < e; i += stride) dst[i] = src[i];
+    const uint4 *vs = reinterpret_cast<const uint4 *>(src);
+    uint4 *vd = reinterpret_cast<uint4 *>(dst);
+    const size_t j1 = a1 / VW;
+    for (size_t j0 = a0 / VW + gtid; j0 < j1; j0 += U * stride) {
+        uint4 q[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u)
+            if (j0 + u * stride < j1) q[u] = vs[j0 + u * stride];
+#pragma unroll
+        for (int u = 0; u < U; ++u)
+            if (j0 + u * stride < j1) vd[j0 + u * stride] = q[u];
+    }
+}
+
 // The scratch regions [0, b_lo) and [b_hi, n) into the array (keys, and
-// values for key-value selects); four elements per thread in flight.
+// values for key-value selects).
 template <typename C, typename V>
 __global__ void __launch_bounds__(256) sel_copyback_kernel(SelArgs a)
 {
     constexpr bool HAS_V = !std::is_same<V, uint8_t>::value;
-    const size_t b_lo = a.st->b_lo, b_hi = a.st->b_lo + a.st->b_n, n = a.n;
-    const size_t m = b_lo + (n - min(b_hi, n));      // elements to move
-    C *keys = static_cast<C *>(a.keys);
-    V *vals = static_cast<V *>(a.vals);
-    const C *scr_k = static_cast<const C *>(a.mis_k);
-    const V *scr_v = static_cast<const V *>(a.mis_v);
+    const size_t n = a.n, b_lo = min((size_t)a.st->b_lo, n);
+    const size_t b_hi = min((size_t)(a.st->b_lo + a.st->b_n), n);
+    const size_t gtid = (size_t)blockIdx.x * 256 + threadIdx.x;
     const size_t stride = (size_t)gridDim.x * 256;
-    constexpr int U = 4;
-    for (size_t j0 = (size_t)blockIdx.x * 256 + threadIdx.x; j0 < m; j0 += U * stride) {
-        C k[U];
-        V v[U];
-#pragma unroll
-        for (int u = 0; u < U; ++u) {
-            const size_t j = j0 + u * stride;
-            const size_t i = j < b_lo ? j : b_hi + (j - b_lo);
-            if (j < m) {
-                k[u] = scr_k[i];
-                if constexpr (HAS_V)
-                    if (a.op == SOP_KV) v[u] = scr_v[i];
-            }
-        }
-#pragma unroll
-        for (int u = 0; u < U; ++u) {
-            const size_t j = j0 + u * stride;
-            const size_t i = j < b_lo ? j : b_hi + (j - b_lo);
-            if (j < m) {
-                keys[i] = k[u];
-                if constexpr (HAS_V)
-                    if (a.op == SOP_KV) vals[i] = v[u];
-            }
+    C *keys = static_cast<C *>(a.keys);
+    const C *scr_k = static_cast<const C *>(a.mis_k);
+    copy_range<C>(keys, scr_k, 0, b_lo, gtid, stride);
+    copy_range<C>(keys, scr_k, b_hi, n, gtid, stride);
+    if constexpr (HAS_V) {
+        if (a.op == SOP_KV) {
+            V *vals = static_cast<V *>(a.vals);
+            const V *scr_v = static_cast<const V *>(a.mis_v);
+            copy_range<V>(vals, scr_v, 0, b_lo, gtid, stride);
+            copy_range<V>(vals, scr_v, b_hi, n, gtid, stride);
         }
     }
 }
