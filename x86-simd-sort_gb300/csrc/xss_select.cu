@@ -18,9 +18,10 @@
 // back into B's region partitioned around K, and a last kernel moves the
 // listed L/G elements into the holes.  Only misplaced elements move, as in
 // an in-place quickselect partition, and the array is read twice.  When k
-// is far from both ends (about half of each side's keys misplaced) the split
-// instead writes every key once to a scratch copy -- L to its front, G to its
-// back -- and the outer regions are copied back (select_launch chooses).
+// is far from both ends (about half of each side's keys misplaced) round 0's
+// read also copies the array to scratch, and the split reads that copy and
+// writes every key once into the array -- L to its front, G to its back
+// (select_launch chooses).
 #include <algorithm>
 #include <cstring>
 #include <type_traits>
@@ -90,15 +91,50 @@ __device__ __forceinline__ uint32_t sel_block_excl_scan(uint32_t v, uint32_t *s_
     return pre + x - v;
 }
 
+// dst[i] = src[i] for i in [s, e) by every thread of the grid (global thread
+// gtid of `stride`): 16-byte vectors, four per thread in flight, over the part
+// of the range that starts on a 16-byte boundary in both arrays; single
+// elements before and after it, and everywhere if the arrays' alignments differ.
+template <typename T>
+__device__ __forceinline__ void copy_range(T *dst, const T *src, size_t s, size_t e, size_t gtid,
+                                           size_t stride)
+{
+    constexpr size_t VW = 16 / sizeof(T);
+    constexpr int U = 4;
+    if (s >= e) return;
+    const bool al = ((reinterpret_cast<uintptr_t>(dst) | reinterpret_cast<uintptr_t>(src)) & 15) == 0;
+    const size_t a0 = al ? std::min(e, (s + VW - 1) / VW * VW) : e;   // first vector element
+    const size_t a1 = al ? std::max(a0, e / VW * VW) : e;             // end of the vectors
+    for (size_t i = s + gtid; i < a0; i += stride) dst[i] = src[i];
+    for (size_t i = a1 + gtid; i < e; i += stride) dst[i] = src[i];
+    const uint4 *vs = reinterpret_cast<const uint4 *>(src);
+    uint4 *vd = reinterpret_cast<uint4 *>(dst);
+    const size_t j1 = a1 / VW;
+    for (size_t j0 = a0 / VW + gtid; j0 < j1; j0 += U * stride) {
+        uint4 q[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u)
+            if (j0 + u * stride < j1) q[u] = vs[j0 + u * stride];
+#pragma unroll
+        for (int u = 0; u < U; ++u)
+            if (j0 + u * stride < j1) vd[j0 + u * stride] = q[u];
+    }
+}
+
 // One histogram round over every key (round 0) or over the compacted
 // candidates (rounds >= 2; round 1 is the split pass).  16-byte vector
 // loads, four per thread in flight, keep enough bytes moving to cover memory
 // latency; an unaligned array takes the scalar loop.  (Issuing each step's
 // loads before the previous step's keys are counted, and interleaved copies
-// of the bins, measured no faster.)
+// of the bins, measured no faster.)  With `copy` set (round 0 of an
+// out-of-place select) the same read also copies the keys into the scratch
+// copy a.mis_k, and a key-value select's values (copy_vb bytes each) into
+// a.mis_v: the split pass then reads the copy and writes the outer classes
+// straight into the caller's arrays, so no copy-back pass is needed.
 template <typename C>
 __global__ void __launch_bounds__(256) sel_hist_kernel(SelArgs a, int round, int lo, int bits,
-                                                       int from_keys)
+                                                       int from_keys, int copy = 0,
+                                                       int copy_vb = 0)
 {
     constexpr int VW = 16 / sizeof(C);   // keys per vector
     constexpr int U = 4;                 // vectors per thread in flight
@@ -121,10 +157,12 @@ __global__ void __launch_bounds__(256) sel_hist_kernel(SelArgs a, int round, int
         if (match) atomicAdd(&sh[uint32_t(c >> lo) & (uint32_t)(nb - 1)], 1u);
     };
 
+    C *dst = copy ? static_cast<C *>(a.mis_k) : nullptr;   // 256-byte aligned scratch
     size_t head = 0;
     if ((reinterpret_cast<uintptr_t>(src) & 15) == 0) {
         const size_t nvec = count / VW;
         const uint4 *vsrc = reinterpret_cast<const uint4 *>(src);
+        uint4 *vdst = reinterpret_cast<uint4 *>(dst);
         for (size_t v0 = wbase; v0 < nvec; v0 += U * stride) {
             uint4 w[U];
 #pragma unroll
@@ -134,7 +172,9 @@ __global__ void __launch_bounds__(256) sel_hist_kernel(SelArgs a, int round, int
             }
 #pragma unroll
             for (int u = 0; u < U; ++u) {
-                const bool act = v0 + lane + u * stride < nvec;
+                const size_t v = v0 + lane + u * stride;
+                const bool act = v < nvec;
+                if (copy && act) vdst[v] = w[u];
                 const C *e = reinterpret_cast<const C *>(&w[u]);
 #pragma unroll
                 for (int j = 0; j < VW; ++j) visit(e[j], act);
@@ -144,7 +184,21 @@ __global__ void __launch_bounds__(256) sel_hist_kernel(SelArgs a, int round, int
     }
     for (size_t i0 = head + wbase; i0 < count; i0 += stride) {
         const size_t i = i0 + lane;
-        visit(i < count ? src[i] : C(0), i < count);
+        const C b = i < count ? src[i] : C(0);
+        if (copy && i < count) dst[i] = b;
+        visit(b, i < count);
+    }
+    if (copy && a.op == SOP_KV && copy_vb) {
+        const size_t gtid = (size_t)blockIdx.x * 256 + threadIdx.x;
+        if (copy_vb == 2)
+            copy_range<uint16_t>(static_cast<uint16_t *>(a.mis_v),
+                                 static_cast<const uint16_t *>(a.vals), 0, count, gtid, stride);
+        else if (copy_vb == 4)
+            copy_range<uint32_t>(static_cast<uint32_t *>(a.mis_v),
+                                 static_cast<const uint32_t *>(a.vals), 0, count, gtid, stride);
+        else if (copy_vb == 8)
+            copy_range<uint64_t>(static_cast<uint64_t *>(a.mis_v),
+                                 static_cast<const uint64_t *>(a.vals), 0, count, gtid, stride);
     }
     __syncthreads();
     for (int i = threadIdx.x; i < nb; i += 256)
@@ -645,17 +699,19 @@ __global__ void __launch_bounds__(256) sel_split_sparse_kernel(SelArgs a, int lo
         if (sh[i]) atomicAdd(&a.st->hist[i], sh[i]);
 }
 
-// Out-of-place three-way split for 32- and 64-bit keys: every key of class L
-// goes to the front of a scratch copy of the array ([0, b_lo)), every key of
-// class G to its back ([b_hi, n)), and B's keys become candidates (codes,
-// with values or positions).  Argselect writes the positions of L and G
-// straight into its output instead of the scratch copy.  For each key slot
-// the warp votes two masks (class L, class G; class B is the rest); a CTA
-// votes SPL_SUB sub-steps (masks kept in shared memory), adds its warps'
-// counts and reserves each output's slots with one global atomic per output,
-// then reloads the keys (from L2) and writes each once, slot = warp base +
-// running count + rank among the lanes of the vote.  No hole lists are kept;
-// sel_copyback_kernel then moves the scratch regions into the array.
+// Out-of-place three-way split for 32- and 64-bit keys.  Round 0's histogram
+// read left a scratch copy of the keys (and of a key-value select's values);
+// this pass reads the copy and writes every key of class L to the front of
+// the caller's array ([0, b_lo)) and every key of class G to its back
+// ([b_hi, n)); B's keys become candidates (codes, with values or positions).
+// Argselect leaves the array alone: it reads the array itself and writes the
+// positions of L and G straight into its output.  For each key slot the warp
+// votes two masks (class L, class G; class B is the rest); a CTA votes
+// SPL_SUB sub-steps (masks kept in shared memory), adds its warps' counts and
+// reserves each output's slots with one global atomic per output, then
+// reloads the keys (from L2) and writes each once, slot = warp base + running
+// count + rank among the lanes of the vote.  No hole lists are kept, and
+// nothing is copied back.
 // The values of the keys spl_load read (same key slots), with vector loads
 // where the value array is aligned to a row of VEC values.
 template <typename C, typename V>
@@ -710,10 +766,12 @@ __global__ void __launch_bounds__(SPL_BLOCK, 2) sel_split3_kernel(SelArgs a, int
     // positions and slots fit 32 bits: selects above XSS_RADIX_MAX_N keys sort
     const uint32_t n = (uint32_t)a.n;
     const uint32_t b_hi = (uint32_t)(a.st->b_lo + a.st->b_n);
-    const C *keys = static_cast<const C *>(a.keys);
-    const V *vals = static_cast<const V *>(a.vals);
-    C *scr_k = static_cast<C *>(a.mis_k);
-    V *scr_v = static_cast<V *>(a.mis_v);
+    // read the scratch copy (argselect: the array), write the array
+    const C *keys = a.op == SOP_ARG ? static_cast<const C *>(a.keys)
+                                    : static_cast<const C *>(a.mis_k);
+    const V *vals = static_cast<const V *>(a.mis_v);
+    C *out_k = static_cast<C *>(a.keys);
+    V *out_v = static_cast<V *>(a.vals);
     C *cand = static_cast<C *>(a.cand);
     uint32_t *cand_pos = static_cast<uint32_t *>(a.cand_p);
     V *cand_val = static_cast<V *>(a.cand_p);
@@ -797,9 +855,9 @@ __global__ void __launch_bounds__(SPL_BLOCK, 2) sel_split3_kernel(SelArgs a, int
                     } else if (a.op == SOP_ARG) {
                         a.out_idx[at] = p;
                     } else {
-                        scr_k[at] = raw[e];
+                        out_k[at] = raw[e];
                         if constexpr (HAS_V)
-                            if (a.op == SOP_KV) scr_v[at] = vv[e];
+                            if (a.op == SOP_KV) out_v[at] = vv[e];
                     }
                 }
                 const uint32_t nL = __popc(mL), nG = __popc(mG);
@@ -813,60 +871,6 @@ __global__ void __launch_bounds__(SPL_BLOCK, 2) sel_split3_kernel(SelArgs a, int
     __syncthreads();
     for (int i = tid; i < nb; i += SPL_BLOCK)
         if (sh[i]) atomicAdd(&a.st->hist[i], sh[i]);
-}
-
-// dst[i] = src[i] for i in [s, e) by every thread of the grid (global thread
-// gtid of `stride`): 16-byte vectors, four per thread in flight, over the part
-// of the range that starts on a 16-byte boundary in both arrays; single
-// elements before and after it, and everywhere if the arrays' alignments differ.
-template <typename T>
-__device__ __forceinline__ void copy_range(T *dst, const T *src, size_t s, size_t e, size_t gtid,
-                                           size_t stride)
-{
-    constexpr size_t VW = 16 / sizeof(T);
-    constexpr int U = 4;
-    if (s >= e) return;
-    const bool al = ((reinterpret_cast<uintptr_t>(dst) | reinterpret_cast<uintptr_t>(src)) & 15) == 0;
-    const size_t a0 = al ? std::min(e, (s + VW - 1) / VW * VW) : e;   // first vector element
-    const size_t a1 = al ? std::max(a0, e / VW * VW) : e;             // end of the vectors
-    for (size_t i = s + gtid; i < a0; i += stride) dst[i] = src[i];
-    for (size_t i = a1 + gtid; i < e; i += stride) dst[i] = src[i];
-    const uint4 *vs = reinterpret_cast<const uint4 *>(src);
-    uint4 *vd = reinterpret_cast<uint4 *>(dst);
-    const size_t j1 = a1 / VW;
-    for (size_t j0 = a0 / VW + gtid; j0 < j1; j0 += U * stride) {
-        uint4 q[U];
-#pragma unroll
-        for (int u = 0; u < U; ++u)
-            if (j0 + u * stride < j1) q[u] = vs[j0 + u * stride];
-#pragma unroll
-        for (int u = 0; u < U; ++u)
-            if (j0 + u * stride < j1) vd[j0 + u * stride] = q[u];
-    }
-}
-
-// The scratch regions [0, b_lo) and [b_hi, n) into the array (keys, and
-// values for key-value selects).
-template <typename C, typename V>
-__global__ void __launch_bounds__(256) sel_copyback_kernel(SelArgs a)
-{
-    constexpr bool HAS_V = !std::is_same<V, uint8_t>::value;
-    const size_t n = a.n, b_lo = min((size_t)a.st->b_lo, n);
-    const size_t b_hi = min((size_t)(a.st->b_lo + a.st->b_n), n);
-    const size_t gtid = (size_t)blockIdx.x * 256 + threadIdx.x;
-    const size_t stride = (size_t)gridDim.x * 256;
-    C *keys = static_cast<C *>(a.keys);
-    const C *scr_k = static_cast<const C *>(a.mis_k);
-    copy_range<C>(keys, scr_k, 0, b_lo, gtid, stride);
-    copy_range<C>(keys, scr_k, b_hi, n, gtid, stride);
-    if constexpr (HAS_V) {
-        if (a.op == SOP_KV) {
-            V *vals = static_cast<V *>(a.vals);
-            const V *scr_v = static_cast<const V *>(a.mis_v);
-            copy_range<V>(vals, scr_v, 0, b_lo, gtid, stride);
-            copy_range<V>(vals, scr_v, b_hi, n, gtid, stride);
-        }
-    }
 }
 
 // B's region rewritten from the candidates, partitioned around K:
@@ -1066,10 +1070,11 @@ static int select_launch(int op, KeyXform xf, void *keys, void *vals, uint64_t *
     const int W = 8 * (int)sizeof(C);
     const int rounds = (W + SEL_DIGIT - 1) / SEL_DIGIT;   // 3 (32-bit) or 6 (64-bit)
     // Where k is not near either end, a good share of the keys on each side
-    // of the bucket lie in the other side's region: writing every key once to
-    // a scratch copy (and copying its outer regions back) costs less than
-    // listing and moving the misplaced ones (qselect float32 2^27, k = 2^26:
-    // 0.76 against 1.38 ms).  Within n / 4096 of an end only a few keys are
+    // of the bucket lie in the other side's region: copying the array to
+    // scratch during round 0's read and writing every key once from the copy
+    // costs less than listing and moving the misplaced ones (qselect float32
+    // 2^27, k = 2^26: 0.76 against 1.38 ms with a copy-back of the outer
+    // regions after the split, which the copy during round 0 replaced).  Within n / 4096 of an end only a few keys are
     // recorded, and the sparse in-place split reads the array at little more
     // than memory speed.
     const bool out_of_place = std::min(k, n - 1 - k) >= n / 4096;
@@ -1094,10 +1099,14 @@ static int select_launch(int op, KeyXform xf, void *keys, void *vals, uint64_t *
             XSS_LAUNCH(PK_SEL_COLLECT, s,
                        (sel_split_sparse_kernel<C, V><<<sg, 256, 0, s>>>(a, lo, bits)));
         } else {
-            // round 0 reads every key; later rounds only the candidates
+            // round 0 reads every key (and, out of place, copies the keys and
+            // a key-value select's values to the scratch copy the split pass
+            // reads); later rounds read only the candidates
             const int g = r >= 2 ? std::max(1, grid / 4) : grid;
+            const int copy = r == 0 && out_of_place && op != SOP_ARG;
             XSS_LAUNCH(PK_SEL_HIST, s,
-                       sel_hist_kernel<C><<<g, 256, 0, s>>>(a, r, lo, bits, r == 0 ? 1 : 0));
+                       sel_hist_kernel<C><<<g, 256, 0, s>>>(a, r, lo, bits, r == 0 ? 1 : 0,
+                                                            copy, op == SOP_KV ? vbytes : 0));
         }
         XSS_CUDA_TRY(cudaGetLastError());
         XSS_LAUNCH(PK_SEL_FIND, s,
@@ -1106,13 +1115,7 @@ static int select_launch(int op, KeyXform xf, void *keys, void *vals, uint64_t *
     }
     XSS_LAUNCH(PK_SEL_PLACE, s, (sel_bpart_kernel<C, V><<<grid, 256, 0, s>>>(a)));
     XSS_CUDA_TRY(cudaGetLastError());
-    if (out_of_place) {
-        if (op != SOP_ARG) {
-            XSS_LAUNCH(PK_SEL_PLACE, s,
-                       (sel_copyback_kernel<C, V><<<sms * 8, 256, 0, s>>>(a)));
-            XSS_CUDA_TRY(cudaGetLastError());
-        }
-    } else {
+    if (!out_of_place) {
         XSS_LAUNCH(PK_SEL_PLACE, s, (sel_place_kernel<C, V><<<grid, 256, 0, s>>>(a, 0)));
         XSS_CUDA_TRY(cudaGetLastError());
     }
