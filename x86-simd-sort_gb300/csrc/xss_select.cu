@@ -709,9 +709,10 @@ __global__ void __launch_bounds__(256) sel_split_sparse_kernel(SelArgs a, int lo
 // votes two masks (class L, class G; class B is the rest); a CTA votes
 // SPL_SUB sub-steps (masks kept in shared memory), adds its warps' counts and
 // reserves each output's slots with one global atomic per output, then
-// reloads the keys (from L2) and writes each once, slot = warp base + running
-// count + rank among the lanes of the vote.  No hole lists are kept, and
-// nothing is copied back.
+// reloads the keys (from L2) and writes each once, slot = warp base + the
+// warp's count of that class before the key slot (stored with the masks) +
+// rank among the lanes of the vote.  No hole lists are kept, and nothing is
+// copied back.
 // The values of the keys spl_load read (same key slots), with vector loads
 // where the value array is aligned to a row of VEC values.
 template <typename C, typename V>
@@ -754,9 +755,13 @@ __global__ void __launch_bounds__(SPL_BLOCK, 2) sel_split3_kernel(SelArgs a, int
     constexpr int E = S::E, VEC = S::VEC;
     constexpr bool HAS_V = !std::is_same<V, uint8_t>::value;
     __shared__ uint32_t sh[SEL_BINS];
-    __shared__ uint32_t s_mask[SPL_SUB][SPL_WARPS][E][2];   // class L, class G
+    // per key slot of a warp: class L mask, class G mask, and the warp's L and G
+    // counts before the slot within the step (16 bits each: a warp's step holds
+    // SPL_SUB * WSUB = 2048 keys)
+    __shared__ uint4 s_ent[SPL_SUB][SPL_WARPS][E];
     __shared__ uint32_t s_cnt[SPL_WARPS][3];
     __shared__ uint32_t s_base[SPL_WARPS][3];
+    static_assert(SPL_SUB * S::WSUB < 65536, "step counts must fit 16 bits");
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int nb = 1 << bits;
     for (int i = tid; i < nb; i += SPL_BLOCK) sh[i] = 0;
@@ -781,7 +786,7 @@ __global__ void __launch_bounds__(SPL_BLOCK, 2) sel_split3_kernel(SelArgs a, int
     const uint32_t lt = (1u << lane) - 1u, bit = 1u << lane;
     const uint32_t lane0 = (uint32_t)lane * VEC;   // lane's first key in a vector row
     for (uint32_t s0 = blockIdx.x * (uint32_t)S::STEP; s0 < n; s0 += gridDim.x * (uint32_t)S::STEP) {
-        uint32_t tL = 0, tG = 0, tC = 0;
+        uint32_t tL = 0, tG = 0, tIn = 0;   // the warp's L, G and in-range keys so far
         C raw[E], nxt[E];
         spl_load<C>(keys, n, s0 + (uint32_t)warp * S::WSUB, lane, vec_ok, nxt);
 #pragma unroll 1
@@ -800,16 +805,18 @@ __global__ void __launch_bounds__(SPL_BLOCK, 2) sel_split3_kernel(SelArgs a, int
                 const bool isL = in && top < pre, isG = in && top > pre;
                 const uint32_t mL = __ballot_sync(0xffffffffu, isL);
                 const uint32_t mG = __ballot_sync(0xffffffffu, isG);
-                if (in && !isL && !isG) atomicAdd(&sh[uint32_t(c >> lo) & (uint32_t)(nb - 1)], 1u);
-                if (lane == 0) s_mask[sub][warp][e][0] = mL;
-                if (lane == 1) s_mask[sub][warp][e][1] = mG;
+                const uint32_t mIn = full ? 0xffffffffu : __ballot_sync(0xffffffffu, in);
+                if (lane == 0) s_ent[sub][warp][e] = make_uint4(mL, mG, tL | (tG << 16), 0u);
+                if ((mL | mG) != mIn) {   // uniform: some lane holds a class-B key
+                    if (in && !isL && !isG)
+                        atomicAdd(&sh[uint32_t(c >> lo) & (uint32_t)(nb - 1)], 1u);
+                }
                 tL += __popc(mL);
                 tG += __popc(mG);
-                tC += full ? 32u - __popc(mL | mG)
-                           : __popc(__ballot_sync(0xffffffffu, in) & ~(mL | mG));
+                tIn += full ? 32u : __popc(mIn);
             }
         }
-        if (lane < 3) s_cnt[warp][lane] = lane == 0 ? tL : (lane == 1 ? tG : tC);
+        if (lane < 3) s_cnt[warp][lane] = lane == 0 ? tL : (lane == 1 ? tG : tIn - tL - tG);
         __syncthreads();
         if (tid < 3) {
             uint32_t sum = 0;
@@ -826,7 +833,8 @@ __global__ void __launch_bounds__(SPL_BLOCK, 2) sel_split3_kernel(SelArgs a, int
             }
         }
         __syncthreads();
-        uint32_t rL = s_base[warp][0], rG = s_base[warp][1], rC = s_base[warp][2];
+        const uint32_t bL = s_base[warp][0], bG = s_base[warp][1], bC = s_base[warp][2];
+        uint32_t inBefore = 0;   // the warp's in-range keys of the step before this slot
 #pragma unroll 1
         for (int sub = 0; sub < SPL_SUB; ++sub) {
             const uint32_t w0 = s0 + (uint32_t)sub * S::SUB + (uint32_t)warp * S::WSUB;
@@ -840,12 +848,16 @@ __global__ void __launch_bounds__(SPL_BLOCK, 2) sel_split3_kernel(SelArgs a, int
             for (int e = 0; e < E; ++e) {
                 const uint32_t p = w0 + (uint32_t)(e / VEC) * (32 * VEC) + lane0 + (e % VEC);
                 const uint32_t act = full ? 0xffffffffu : __ballot_sync(0xffffffffu, p < n);
-                const uint32_t mL = s_mask[sub][warp][e][0], mG = s_mask[sub][warp][e][1];
+                const uint4 ent = s_ent[sub][warp][e];
+                const uint32_t mL = ent.x, mG = ent.y;
+                const uint32_t pL = ent.z & 0xFFFFu, pG = ent.z >> 16;
                 const uint32_t mC = act & ~(mL | mG);
                 // this key's class mask and slot; one store path per output kind
                 const bool inL = mL & bit, inG = mG & bit;
                 const uint32_t m = inL ? mL : (inG ? mG : mC);
-                const uint32_t at = (inL ? rL : (inG ? rG : rC)) + __popc(m & lt);
+                const uint32_t at = (inL ? bL + pL : (inG ? bG + pG : bC + inBefore - pL - pG)) +
+                                    __popc(m & lt);
+                inBefore += full ? 32u : __popc(act);
                 if ((act & bit) && at < n) {
                     if (!inL && !inG) {
                         cand[at] = cx.to(raw[e]);
@@ -860,13 +872,9 @@ __global__ void __launch_bounds__(SPL_BLOCK, 2) sel_split3_kernel(SelArgs a, int
                             if (a.op == SOP_KV) out_v[at] = vv[e];
                     }
                 }
-                const uint32_t nL = __popc(mL), nG = __popc(mG);
-                rL += nL;
-                rG += nG;
-                rC += full ? 32u - nL - nG : __popc(mC);
             }
         }
-        __syncthreads();   // s_mask / s_cnt / s_base are rewritten by the next step
+        __syncthreads();   // s_ent / s_cnt / s_base are rewritten by the next step
     }
     __syncthreads();
     for (int i = tid; i < nb; i += SPL_BLOCK)
