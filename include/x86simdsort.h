@@ -219,6 +219,10 @@ void object_qsort(T *d_arr, size_t n, K T::*key, bool hasnan = false, bool desce
 // Wait for `stream` and report a device-side error latched by earlier calls.
 inline void synchronize(xss_stream_t stream = nullptr) { check(xss_gpu_stream_status(stream)); }
 
+// Free the device memory the library caches between calls on the current
+// device (every stream's workspace, this thread's host-pointer buffers).
+inline void release_cached() { check(xss_release_cached()); }
+
 }  // namespace gpu
 }  // namespace x86simdsort
 

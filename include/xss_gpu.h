@@ -77,6 +77,21 @@ const char *xss_version(void);
 size_t xss_gpu_workspace_size(int op, int key_dtype, int val_dtype, size_t n, size_t k);
 
 /*
+ * Frees the device memory the library keeps between calls on the current
+ * device: the cached workspaces of every stream (device-pointer calls given
+ * d_ws = NULL, and the device record sort), and the calling thread's staging
+ * and pipeline buffers of host-pointer calls (each thread that makes
+ * host-pointer calls holds its own, up to about twice the bytes of its
+ * largest array).  Waits for all work on the device first.  Buffers of other
+ * threads' host-pointer calls stay: each thread releases its own, e.g. before
+ * it exits.  Later calls allocate again as needed.  Not to be called while
+ * another thread is inside a call of this library on the same device.
+ * Returns XSS_OK or XSS_ECUDA.  No counterpart in the reference library (a CPU
+ * library keeps no device memory).
+ */
+int xss_release_cached(void);
+
+/*
  * Device-pointer calls are asynchronous.  Kernels that give up a bounded wait
  * latch an error word on the device; this call synchronises `stream`, reads
  * and clears that word and returns XSS_OK, XSS_ETIMEOUT or XSS_ECUDA.

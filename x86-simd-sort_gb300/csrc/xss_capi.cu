@@ -466,6 +466,35 @@ size_t xss_gpu_workspace_size(int op, int key_dtype, int val_dtype, size_t n, si
 
 int xss_gpu_stream_status(xss_stream_t stream) { return stream_status((cudaStream_t)stream); }
 
+int xss_release_cached(void)
+{
+    using namespace xss;
+    // the cached buffers may be in use by work queued on any stream, including
+    // streams the caller has destroyed since: wait for the whole device
+    if (cudaDeviceSynchronize() != cudaSuccess) return XSS_ECUDA;
+    const int d = cur_device();
+    bool ok = true;
+    {
+        std::lock_guard<std::mutex> lk(g_mu);
+        for (auto it = g_ws.begin(); it != g_ws.end();) {
+            if (it->first.first == d) {
+                if (it->second.p && cudaFree(it->second.p) != cudaSuccess) ok = false;
+                it = g_ws.erase(it);
+            } else {
+                ++it;
+            }
+        }
+    }
+    HostCtx &c = t_ctx[d];
+    for (int i = 0; i < 3; ++i) {
+        if (c.buf[i] && cudaFree(c.buf[i]) != cudaSuccess) ok = false;
+        c.buf[i] = nullptr;
+        c.cap[i] = 0;
+    }
+    if (!release_pipeline_buffer()) ok = false;
+    return ok ? XSS_OK : XSS_ECUDA;
+}
+
 int xss_gpu_qsort(int dtype, void *d_arr, size_t n, int hasnan, int descending, void *d_ws,
                   size_t ws_bytes, xss_stream_t stream)
 {

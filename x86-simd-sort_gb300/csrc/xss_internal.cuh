@@ -99,6 +99,10 @@ bool host_pipeline_wanted(size_t n);
 void touch_host_pages(const void *p, size_t bytes);
 int host_pipelined_sort(int op, int kbytes, KeyXform xf, void *hk, void *hv, int vbytes,
                         uint64_t *hidx, size_t n);
+// Free the calling thread's pipeline buffer on the current device (its
+// streams stay); the caller has synchronised the device.  False if the free
+// failed.
+bool release_pipeline_buffer();
 
 // Keys-only sorts of 16-bit keys above COUNT16_MIN_N keys count every code
 // instead of radix sorting (xss_count16.cu); radix_sort, radix_select and

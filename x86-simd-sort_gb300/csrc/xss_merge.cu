@@ -411,6 +411,17 @@ static int pipe_ctx(PipeCtx *&c, size_t bytes)
 
 bool host_pipeline_wanted(size_t n) { return n >= PIPE_MIN_N; }
 
+bool release_pipeline_buffer()
+{
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return false;
+    PipeCtx &c = t_pipe[dev];
+    const bool ok = c.buf == nullptr || cudaFree(c.buf) == cudaSuccess;
+    c.buf = nullptr;
+    c.cap = 0;
+    return ok;
+}
+
 template <typename C, typename V>
 static int pipelined_sort_c(int op, KeyXform xf, C *hk, V *hv, uint64_t *hidx, size_t n)
 {

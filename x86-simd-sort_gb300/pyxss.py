@@ -49,6 +49,7 @@ _SIGS = {
     "xss_version": (ctypes.c_char_p, []),
     "xss_gpu_workspace_size": (_Z, [_I, _I, _I, _Z, _Z]),
     "xss_gpu_stream_status": (_I, [_P]),
+    "xss_release_cached": (_I, []),
     "xss_gpu_qsort": (_I, [_I, _P, _Z, _I, _I, _P, _Z, _P]),
     "xss_gpu_qselect": (_I, [_I, _P, _Z, _Z, _I, _I, _P, _Z, _P]),
     "xss_gpu_partial_qsort": (_I, [_I, _P, _Z, _Z, _I, _I, _P, _Z, _P]),
@@ -212,6 +213,13 @@ def workspace_size(op: str, key_dtype, n: int, k: int = 0, val_dtype="uint64") -
 
 def stream_status(stream: int = 0) -> None:
     check(lib().xss_gpu_stream_status(stream or None), "device status")
+
+
+def release_cached() -> None:
+    """Free the library's cached device buffers on the current device (every
+    stream's workspace, this thread's host-pointer staging and pipeline
+    buffers)."""
+    check(lib().xss_release_cached(), "release cached")
 
 
 def gpu_qsort(dt, d_arr: int, n: int, hasnan=False, descending=False, ws=0, ws_bytes=0,
