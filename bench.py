@@ -1105,9 +1105,98 @@ class SegmentedF32(SegmentedSort):
     name = "segmented_f32"
     kdt, kid = "float32", 5
 
+
+class SegmentedTopk(SegmentedSort):
+    """Batched top-k over the config-4 segments (int32 keys -> uint32 local
+    index): every segment's k smallest keys, in order, at its front
+    (xss_gpu_segmented_topk).  Segments up to 4096 keys are sorted whole on
+    chip; longer ones are streamed once by one CTA each (k <= 2048)."""
+
+    name = "segmented_topk"
+    default_k = 1000
+    dominant = None
+    has_percall = False
+    roofline_name = "segmented top-k (all kernels of one call)"
+
+    def describe(self):
+        d = super().describe()
+        d["workload"] = d["workload"].replace("segmented keyvalue sort",
+                                              f"segmented keyvalue top-k, k={self.k},")
+        d["k"] = self.k
+        return d
+
+    def run(self):
+        self.xss.gpu_segmented_topk(self.kdt, "uint32", self.kk.data_ptr(), self.v.data_ptr(),
+                                    self.doff.data_ptr(), self.off, self.sizes.size, self.k,
+                                    False, False, self.ws.data_ptr(), self.wsb,
+                                    self.stream.cuda_stream)
+
+    def setup(self):
+        topk = self.k
+        super().setup()                  # names the key buffer self.k
+        self.kk, self.k = self.k, topk   # key buffer; the workload's k
+
+    def restore(self):
+        self.kk.copy_(self.k0)
+        self.v.copy_(self.v0)
+
+    def check(self, samples=300):
+        rng = np.random.default_rng(11)
+        picks = set(rng.integers(0, self.sizes.size, samples).tolist())
+        picks.update(np.argsort(self.sizes)[-3:].tolist())
+        for s in picks:
+            b, e = int(self.off[s]), int(self.off[s + 1])
+            m = min(self.k, e - b)
+            k = self.kk[b:e].cpu().numpy()
+            v = self.v[b:e].cpu().numpy().view(np.uint32)
+            k0 = self.k0[b:e].cpu().numpy()
+            if not (np.array_equal(k[:m], np.sort(k0)[:m])
+                    and np.array_equal(np.sort(v), np.arange(e - b))
+                    and np.array_equal(k0[v.astype(np.int64)], k)):
+                return False
+        return True
+
+    def cpu_run(self, lib, kind, sample, threads):
+        """The reference's way: one keyvalue_partial_sort(k) call per segment,
+        on the first segments holding about m keys (single-threaded: the
+        reference's partial sorts are not task-parallel)."""
+        m = self._cpu_m
+        stop = int(np.searchsorted(self.off, m))
+        rng = np.random.default_rng(3)
+        k = rng.integers(-2**31, 2**31 - 1, int(self.off[stop]), dtype=np.int32)
+        v = np.zeros(k.size, np.uint32)
+        for s in range(stop):
+            b, e = int(self.off[s]), int(self.off[s + 1])
+            v[b:e] = np.arange(e - b, dtype=np.uint32)
+        for s in range(stop):
+            b, e = int(self.off[s]), int(self.off[s + 1])
+            if e - b <= 1:
+                continue
+            rc = lib.keyvalue_partial_sort(self.kid, 3, k[b:].ctypes.data, v[b:].ctypes.data,
+                                           min(self.k, e - b), e - b, 0, 0)
+            assert rc == 0
+        return int(self.off[stop])
+
+    def passes(self):
+        return 1
+
+    def bytes_model(self):
+        """One read of every key of the streamed segments; a read and a write
+        of keys and values for the segments sorted whole, for each streamed
+        segment's first 4096 keys and for its k results."""
+        small = self.sizes[self.sizes <= 4096]
+        big = self.sizes[self.sizes > 4096]
+        rw = self.kb + self.vb
+        return int(2 * small.sum() * rw + big.sum() * self.kb +
+                   big.size * 2 * (4096 + self.k) * rw)
+
+    def bytes_per_pass(self):
+        return self.bytes_model()
+
 SEG_LITERAL = -1
 DTYPE_OF = {"keyvalue_qsort": "int64", "qsort_f32": "f32", "segmented": "int32",
             "qsort_f32_2e20": "f32", "argsort_i64": "int64", "argsort_f64": "f64",
+            "segmented_topk": "int32",
             "qselect_f32": "f32", "partial_f32": "f32", "segmented_f32": "f32",
             "qselect_u16_zipf": "u16", "qselect_f16_zipf": "f16", "kv_select_f32": "f32",
             "kv_partial_i32": "int32", "argselect_f32": "f32", "object_records": "f32",
@@ -1118,6 +1207,7 @@ WORKLOADS = {"keyvalue_qsort": (KeyValueSort, 1 << 28), "qsort_f32": (QsortF32, 
              "argsort_i64": (ArgsortWorkload, 1 << 28), "argsort_f64": (ArgsortF64, 1 << 28),
              "qselect_f32": (SelectWorkload, 1 << 27), "partial_f32": (PartialWorkload, 1 << 27),
              "segmented_f32": (SegmentedF32, SEG_LITERAL),
+             "segmented_topk": (SegmentedTopk, SEG_LITERAL),
              "qselect_u16_zipf": (SelectZipf16, 1 << 28),
              "qselect_f16_zipf": (SelectZipfF16, 1 << 28),
              "kv_select_f32": (KeyValueSelectWorkload, 1 << 27),
@@ -1559,7 +1649,7 @@ def measure(args, ctx, workload, n_override, steps, warmup, do_e2e=True, do_cpu=
             kernels[kind] = {"ms_per_step": k_ms / steps, "launches_per_step": k_n / steps}
     dom_ms, dom_launches = xss.prof_read(wl.dominant) if wl.dominant else (0.0, 0)
     dom_steps = steps
-    if dom_launches == 0 and hasattr(wl, "run_nograph"):
+    if dom_launches == 0 and wl.dominant and hasattr(wl, "run_nograph"):
         # kernels inside a replayed graph cannot be bracketed by events: time
         # the dominant kernel in one untimed run of the same launch sequence
         with torch.cuda.stream(stream):
@@ -1582,7 +1672,8 @@ def measure(args, ctx, workload, n_override, steps, warmup, do_e2e=True, do_cpu=
     xss.stream_status(stream.cuda_stream)
     checked = wl.check()
     percall = None
-    if hasattr(wl, "run_percall") and percall_segments is not None:
+    if (hasattr(wl, "run_percall") and getattr(wl, "has_percall", True)
+            and percall_segments is not None):
         percall = wl.percall_leg(percall_segments)
 
     if dist is not None:
@@ -1598,7 +1689,7 @@ def measure(args, ctx, workload, n_override, steps, warmup, do_e2e=True, do_cpu=
     kernel_name = "onesweep radix pass"
     if wl.dominant is None:
         # select: several short kernels; the roofline covers the whole operation
-        kernel_name = "select (all kernels of one call)"
+        kernel_name = getattr(wl, "roofline_name", "select (all kernels of one call)")
         avg_pass_ms = ms_per_step
         achieved = wl.bytes_model() / (ms_per_step / 1e3) / 1e9
         active = launches / steps

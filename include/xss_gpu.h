@@ -208,7 +208,11 @@ size_t xss_gpu_segmented_workspace_size(int key_dtype, int val_dtype,
  * partial_qsort per segment, with the reference's partial_qsort semantics
  * (lib/x86simdsort.h:27-29).  Runs in the batched segmented launch: segments
  * up to 4096 keys are sorted on chip whole (which costs no more than their
- * top k), larger segments by the segmented radix sort.  k == 0: no-op.
+ * top k).  For k <= 2048 each longer segment is read once by one CTA, which
+ * keeps the best k so far on chip and merges in only the keys below the
+ * current k-th (their places in the segment take the keys they displace);
+ * for a larger k the longer segments are sorted by the segmented radix sort.
+ * k == 0: no-op.  Workspace: xss_gpu_segmented_workspace_size is enough.
  */
 int xss_gpu_segmented_topk(int key_dtype, int val_dtype, void *d_keys, void *d_vals,
                            const uint64_t *d_offsets, const uint64_t *h_offsets,

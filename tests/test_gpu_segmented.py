@@ -166,3 +166,39 @@ def test_segmented_topk(xss, cuda, kdt, vdt, k):
             assert_same_sorted(ref_sorted(ko[b:e]), ref_sorted(keys[b:e]), what + " multiset")
             if vdt:
                 assert_pairs_preserved(keys[b:e], vals[b:e], ko[b:e], vo[b:e], what)
+
+
+@pytest.mark.parametrize("shape", ["reverse", "sorted", "constant", "smallrange"])
+@pytest.mark.parametrize("k", [1, 1000, 2048, 2049])
+def test_segmented_topk_streamed_shapes(xss, cuda, shape, k):
+    """Segments above 4096 keys take the streamed top-k for k <= 2048 (one read
+    of the segment, keys below the running k-th staged and merged on chip) and
+    the full segmented sort above it.  Reversed input (sorted input when
+    descending) makes every key a candidate and merges every window; constant
+    input stages nothing."""
+    torch = cuda
+    sizes = [0, 1, 100, 4096, 4097, 6000, 6144, 10000, 65536, 130001, 5000, 8193]
+    off = np.zeros(len(sizes) + 1, np.uint64)
+    off[1:] = np.cumsum(np.array(sizes, dtype=np.uint64))
+    n = int(off[-1])
+    for kdt, vdt in (("int32", "uint32"), ("float64", None), ("uint16", "uint64")):
+        keys = get_array(shape, kdt, n, 17)
+        vals = kv_values(vdt, n, 17) if vdt else None
+        for desc in (False, True):
+            dk, dv = _dev(torch, keys), (_dev(torch, vals) if vdt else None)
+            doff = _dev(torch, off)
+            xss.gpu_segmented_topk(kdt, vdt, dk.data_ptr(), dv.data_ptr() if vdt else 0,
+                                   doff.data_ptr(), off, off.size - 1, k, False, desc)
+            xss.stream_status()
+            ko = dk.cpu().numpy().view(keys.dtype)
+            vo = dv.cpu().numpy().view(vals.dtype) if vdt else None
+            for i in range(off.size - 1):
+                b, e = int(off[i]), int(off[i + 1])
+                if e == b:
+                    continue
+                m = min(k, e - b)
+                what = f"topk {shape} {kdt}/{vdt} k={k} desc={desc} seg {i} len {e - b}"
+                assert_same_sorted(ko[b:b + m], ref_sorted(keys[b:e], desc)[:m], what)
+                assert_same_sorted(ref_sorted(ko[b:e]), ref_sorted(keys[b:e]), what + " multiset")
+                if vdt:
+                    assert_pairs_preserved(keys[b:e], vals[b:e], ko[b:e], vo[b:e], what)

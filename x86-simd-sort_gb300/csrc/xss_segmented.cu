@@ -58,6 +58,7 @@ struct SegArgs {
     uint32_t L, T;
     int passes;
     unsigned *err;
+    uint32_t topk;               // top-k plans: k (segments above 4096 keys)
 };
 
 // ---- <= 32 keys: one warp per segment -------------------------------------
@@ -128,6 +129,140 @@ __global__ void __launch_bounds__(SEG_MED_BLOCK) seg_radix_kernel(SegArgs a)
     V *vals = nullptr;
     if constexpr (!std::is_same<V, NoVal>::value) vals = static_cast<V *>(a.vals) + off;
     block_radix_sort<C, V, SEG_MED_BLOCK, ITEMS>(keys, vals, len, (int)sizeof(C), a.xf, s_raw);
+}
+
+// ---- top-k of a segment longer than 4096 keys: one CTA streams it once ------
+// For k <= SEG_TOPK_MAX (the segment's k smallest codes, in order, at its
+// front; the other keys anywhere in the rest of it).  The CTA sorts the
+// segment's first SEG_MED_MAX keys on chip (block_radix_sort) and writes them
+// back: the first k are the best k so far, and thr (the code of the k-th)
+// bounds what can still enter.  It then reads the rest in windows of
+// SEG_TOPK_W positions; a key whose code is below thr is staged, raw, in the
+// block sort's own tile after the best k (its position kept in `cpos`), and
+// every other key stays where it is.  When the stage would overflow, and at
+// the end, the best k are read back in front of the staged keys, the tile is
+// sorted (stable), the first k go back to the segment's front and the rest
+// into the positions the staged keys came from; thr tightens.  Each key is
+// read once and written only if it was staged, so the pass is bound by
+// reading the segment, not by four radix passes.  Keys equal to thr are not
+// staged: any of the tied keys completes the k smallest.
+constexpr uint32_t SEG_TOPK_MAX = SEG_MED_MAX / 2;   // 2048: a stage of >= one window
+constexpr int SEG_TOPK_WI = 8;                        // window items per thread
+constexpr uint32_t SEG_TOPK_W = SEG_MED_BLOCK * SEG_TOPK_WI;   // 2048 positions
+
+template <typename C, typename V> constexpr size_t seg_topk_smem()
+{
+    return block_radix_smem<C, V, SEG_MED_BLOCK, SEG_MED_ITEMS>() +
+           (size_t)SEG_MED_MAX * sizeof(uint32_t) + 32 * sizeof(uint32_t);
+}
+
+template <typename C, typename V>
+__global__ void __launch_bounds__(SEG_MED_BLOCK) seg_topk_kernel(SegArgs a)
+{
+    constexpr int BLOCK = SEG_MED_BLOCK, ITEMS = SEG_MED_ITEMS, WI = SEG_TOPK_WI;
+    constexpr uint32_t TILE = SEG_MED_MAX;
+    constexpr bool HAS_V = !std::is_same<V, NoVal>::value;
+    using VS = typename std::conditional<HAS_V, V, uint8_t>::type;
+    static_assert((uint32_t)BLOCK * ITEMS == TILE, "the tile is the block sort's capacity");
+    static_assert(SEG_TOPK_W <= TILE - SEG_TOPK_MAX, "a window's keys always fit the stage");
+    extern __shared__ __align__(16) unsigned char s_raw[];
+    C *s_k = reinterpret_cast<C *>(s_raw);   // the block sort's key tile
+    VS *s_v = reinterpret_cast<VS *>(s_raw + round16((size_t)TILE * sizeof(C)));
+    uint32_t *cpos = reinterpret_cast<uint32_t *>(
+        s_raw + block_radix_smem<C, V, BLOCK, ITEMS>());   // [TILE - k] staged positions
+    uint32_t *s_scan = cpos + TILE;                          // [32]
+
+    const uint32_t s = a.list[blockIdx.x];
+    const uint64_t off = a.offsets[s];
+    const uint32_t len = (uint32_t)(a.offsets[s + 1] - off);   // > TILE by the plan
+    const uint32_t K = a.topk;                                   // 1 .. SEG_TOPK_MAX
+    C *keys = static_cast<C *>(a.keys) + off;
+    VS *vals = nullptr;
+    if constexpr (HAS_V) vals = static_cast<V *>(a.vals) + off;
+    const int tid = threadIdx.x;
+    if (len <= TILE || K == 0 || K > SEG_TOPK_MAX) return;   // the plan never sends these
+
+    // the first TILE keys, sorted on chip and written back
+    for (uint32_t e = tid; e < TILE; e += BLOCK) {
+        s_k[e] = keys[e];
+        if constexpr (HAS_V) s_v[e] = vals[e];
+    }
+    __syncthreads();
+    block_radix_sort<C, V, BLOCK, ITEMS>(s_k, reinterpret_cast<V *>(s_v), TILE, (int)sizeof(C),
+                                         a.xf, s_raw);
+    __syncthreads();
+    for (uint32_t e = tid; e < TILE; e += BLOCK) {
+        keys[e] = s_k[e];
+        if constexpr (HAS_V) vals[e] = s_v[e];
+    }
+    C thr = to_code(s_k[K - 1], a.xf);
+    __syncthreads();   // the stage below reuses s_k beyond the best k
+
+    const uint32_t cap = TILE - K;
+    uint32_t cnt = 0;   // staged keys (uniform across the CTA)
+    // merge the stage into the best k; the evicted keys fill the stage's holes
+    auto flush = [&]() {
+        __syncthreads();   // every staged key and position is in shared memory
+        for (uint32_t e = tid; e < K; e += BLOCK) {
+            s_k[e] = keys[e];
+            if constexpr (HAS_V) s_v[e] = vals[e];
+        }
+        __syncthreads();
+        block_radix_sort<C, V, BLOCK, ITEMS>(s_k, reinterpret_cast<V *>(s_v), K + cnt,
+                                             (int)sizeof(C), a.xf, s_raw);
+        __syncthreads();
+        for (uint32_t e = tid; e < K; e += BLOCK) {
+            keys[e] = s_k[e];
+            if constexpr (HAS_V) vals[e] = s_v[e];
+        }
+        for (uint32_t i = tid; i < cnt; i += BLOCK) {
+            const uint32_t p = cpos[i];
+            if (p < len) {
+                keys[p] = s_k[K + i];
+                if constexpr (HAS_V) vals[p] = s_v[K + i];
+            }
+        }
+        thr = to_code(s_k[K - 1], a.xf);
+        __syncthreads();   // s_k and cpos are restaged next
+        cnt = 0;
+    };
+
+    for (uint32_t p0 = TILE; p0 < len; p0 += SEG_TOPK_W) {
+        C raw[WI], code[WI];
+#pragma unroll
+        for (int j = 0; j < WI; ++j) {
+            const uint32_t p = p0 + (uint32_t)j * BLOCK + tid;
+            raw[j] = p < len ? keys[p] : C(0);
+            code[j] = to_code(raw[j], a.xf);
+        }
+        uint32_t mine = 0;
+#pragma unroll
+        for (int j = 0; j < WI; ++j)
+            mine += (p0 + (uint32_t)j * BLOCK + tid < len && code[j] < thr) ? 1u : 0u;
+        uint32_t tot;
+        uint32_t at = block_excl_scan<BLOCK>(mine, s_scan, tot);
+        if (cnt + tot > cap) {   // uniform: merge first, then stage against the new bound
+            flush();
+            mine = 0;
+#pragma unroll
+            for (int j = 0; j < WI; ++j)
+                mine += (p0 + (uint32_t)j * BLOCK + tid < len && code[j] < thr) ? 1u : 0u;
+            at = block_excl_scan<BLOCK>(mine, s_scan, tot);
+        }
+        at += cnt;
+#pragma unroll
+        for (int j = 0; j < WI; ++j) {
+            const uint32_t p = p0 + (uint32_t)j * BLOCK + tid;
+            if (p < len && code[j] < thr && at < cap) {
+                s_k[K + at] = raw[j];
+                if constexpr (HAS_V) s_v[K + at] = vals[p];
+                cpos[at] = p;
+                ++at;
+            }
+        }
+        cnt += tot;
+    }
+    if (cnt) flush();
 }
 
 // ---- large segments: histogram of every pass per segment ---------------------
@@ -271,7 +406,8 @@ __global__ void __launch_bounds__(BLOCK, MINB) seg_pass_kernel(SegArgs a, int pa
 // ---------------------------------------------------------------------------
 // Host side: plan = segments binned by size, tile map of the large class.
 struct SegLayout {
-    size_t warp, small, med, lids, ltile0, tlarge, hist, start, status, ctr, tkeys, tvals, total;
+    size_t warp, small, med, lids, ltile0, tlarge, hist, start, status, ctr, tkeys, tvals, tk,
+        total;
 };
 
 struct SegPlan {
@@ -281,6 +417,10 @@ struct SegPlan {
     size_t tile;
     std::vector<uint32_t> warp, small, med, lids, ltile0, tlarge;
     size_t med1 = 0;    // the first med1 entries of med hold <= SEG_MED1_MAX keys
+    // top-k plans (1 <= topk <= SEG_TOPK_MAX): segments above SEG_MED_MAX keys
+    // go to `tk` (seg_topk_kernel) instead of the segmented radix sort
+    uint32_t topk = 0;
+    std::vector<uint32_t> tk;
     SegLayout lay;
     // graph cache for one (keys, vals, offsets, workspace) binding
     cudaGraphExec_t exec = nullptr;
@@ -340,6 +480,7 @@ static int plan_build(SegPlan &p, const uint64_t *off, size_t nseg)
     p.total_n = nseg ? off[nseg] : 0;
     p.tile = seg_tile_size(p.kb, p.vb);
     p.warp.clear(); p.small.clear(); p.med.clear(); p.lids.clear(); p.ltile0.clear(); p.tlarge.clear();
+    p.tk.clear();
     std::vector<uint32_t> med2;
     for (size_t i = 0; i < nseg; ++i) {
         if (off[i + 1] < off[i]) return XSS_EINVAL;
@@ -350,6 +491,7 @@ static int plan_build(SegPlan &p, const uint64_t *off, size_t nseg)
         else if (len <= SEG_SMALL_MAX) p.small.push_back((uint32_t)i);
         else if (len <= SEG_MED1_MAX) p.med.push_back((uint32_t)i);
         else if (len <= SEG_MED_MAX) med2.push_back((uint32_t)i);
+        else if (p.topk) p.tk.push_back((uint32_t)i);
         else {
             p.ltile0.push_back((uint32_t)p.tlarge.size());
             const uint32_t l = (uint32_t)p.lids.size();
@@ -378,6 +520,7 @@ static int plan_build(SegPlan &p, const uint64_t *off, size_t nseg)
     // the large class ping-pongs through mirrors of the whole batch
     y.tkeys = take(L ? p.total_n * p.kb : 0);
     y.tvals = take(L && p.vb ? p.total_n * p.vb : 0);
+    y.tk = take(p.tk.size() * 4);
     y.total = o;
     return XSS_OK;
 }
@@ -416,7 +559,7 @@ static int seg_launch(const SegPlan &p, SegArgs a, cudaStream_t s)
     constexpr size_t TILE = (size_t)BLOCK * ITEMS;
     constexpr bool HAS_V = !std::is_same<V, NoVal>::value;
     const bool any_small = !p.warp.empty() || !p.small.empty() || !p.med.empty();
-    const bool any_large = !p.lids.empty();
+    const bool any_large = !p.lids.empty() || !p.tk.empty();
     SideStream *side = nullptr;
     cudaStream_t ss = s;
     if (any_small && any_large) {
@@ -471,7 +614,21 @@ static int seg_launch(const SegPlan &p, SegArgs a, cudaStream_t s)
         XSS_LAUNCH(PK_SEG_BLOCK, ss, (kern<<<b.count, SEG_MED_BLOCK, smem, ss>>>(b)));
         XSS_CUDA_TRY(cudaGetLastError());
     }
-    if (any_large) {
+    if (!p.tk.empty()) {
+        SegArgs b = a;
+        b.list = reinterpret_cast<const uint32_t *>(ws + p.lay.tk);
+        b.count = (uint32_t)p.tk.size();
+        b.topk = p.topk;
+        const size_t smem = seg_topk_smem<C, V>();
+        auto kern = seg_topk_kernel<C, V>;
+        {
+            const int rc = set_max_dyn_smem((const void *)kern, smem);
+            if (rc) return rc;
+        }
+        XSS_LAUNCH(PK_SEG_BLOCK, s, (kern<<<b.count, SEG_MED_BLOCK, smem, s>>>(b)));
+        XSS_CUDA_TRY(cudaGetLastError());
+    }
+    if (!p.lids.empty()) {
         SegArgs b = a;
         b.large_ids = reinterpret_cast<const uint32_t *>(ws + p.lay.lids);
         b.large_tile0 = reinterpret_cast<const uint32_t *>(ws + p.lay.ltile0);
@@ -535,8 +692,9 @@ static int dtype_kind(int dt, int &kb, int &kind)
 }
 
 static int plan_init(SegPlan &p, int key_dtype, int val_dtype, const uint64_t *h_offsets,
-                     size_t nseg, int hasnan, int descending)
+                     size_t nseg, int hasnan, int descending, uint32_t topk = 0)
 {
+    p.topk = topk;
     int rc = dtype_kind(key_dtype, p.kb, p.kind);
     if (rc) return rc;
     p.key_dtype = key_dtype;
@@ -562,7 +720,8 @@ static int plan_upload(SegPlan &p, char *ws, cudaStream_t s)
     int rc;
     if ((rc = up(p.lay.warp, p.warp)) || (rc = up(p.lay.small, p.small)) ||
         (rc = up(p.lay.med, p.med)) || (rc = up(p.lay.lids, p.lids)) ||
-        (rc = up(p.lay.ltile0, p.ltile0)) || (rc = up(p.lay.tlarge, p.tlarge)))
+        (rc = up(p.lay.ltile0, p.ltile0)) || (rc = up(p.lay.tlarge, p.tlarge)) ||
+        (rc = up(p.lay.tk, p.tk)))
         return rc;
     // pageable copies: make sure they are done before the vectors can change
     XSS_CUDA_TRY(cudaStreamSynchronize(s));
@@ -731,16 +890,42 @@ int xss_gpu_segmented_sort(int key_dtype, int val_dtype, void *d_keys, void *d_v
     return plan_enqueue(p, d_keys, d_vals, d_offsets, s);
 }
 
-// Segmented top-k: the batched sort meets the contract (each segment's k
-// smallest in order at its front) for every k.
+// Segmented top-k.  For k <= SEG_TOPK_MAX the plan sorts segments of up to
+// SEG_MED_MAX keys whole on chip (no more work than their top k) and streams
+// each longer segment once through seg_topk_kernel; a larger k sorts the
+// batch (a sorted segment meets the contract for every k).
 int xss_gpu_segmented_topk(int key_dtype, int val_dtype, void *d_keys, void *d_vals,
                            const uint64_t *d_offsets, const uint64_t *h_offsets,
                            size_t num_segments, size_t k, int hasnan, int descending,
                            void *d_ws, size_t ws_bytes, xss_stream_t stream)
 {
     if (k == 0 || num_segments == 0) return XSS_OK;
-    return xss_gpu_segmented_sort(key_dtype, val_dtype, d_keys, d_vals, d_offsets, h_offsets,
-                                  num_segments, hasnan, descending, d_ws, ws_bytes, stream);
+    if (k > SEG_TOPK_MAX)
+        return xss_gpu_segmented_sort(key_dtype, val_dtype, d_keys, d_vals, d_offsets, h_offsets,
+                                      num_segments, hasnan, descending, d_ws, ws_bytes, stream);
+    cudaStream_t s = (cudaStream_t)stream;
+    std::vector<uint64_t> off;
+    if (!h_offsets) {
+        if (!d_offsets) return XSS_EINVAL;
+        off.resize(num_segments + 1);
+        XSS_CUDA_TRY(cudaMemcpyAsync(off.data(), d_offsets, off.size() * 8,
+                                     cudaMemcpyDeviceToHost, s));
+        XSS_CUDA_TRY(cudaStreamSynchronize(s));
+        h_offsets = off.data();
+    }
+    SegPlan p;
+    int rc = plan_init(p, key_dtype, d_vals ? val_dtype : -1, h_offsets, num_segments, hasnan,
+                       descending, (uint32_t)k);
+    if (rc) return rc;
+    if (!d_ws) {
+        rc = cached_workspace(s, p.lay.total, &d_ws);
+        if (rc) return rc;
+        ws_bytes = p.lay.total;
+    }
+    if (ws_bytes < p.lay.total) return XSS_ENOMEM;
+    rc = plan_upload(p, static_cast<char *>(d_ws), s);
+    if (rc) return rc;
+    return plan_enqueue(p, d_keys, d_vals, d_offsets, s);
 }
 
 // The same batch sorted by one call of the single-array entry point per
