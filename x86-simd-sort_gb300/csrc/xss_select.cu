@@ -1081,10 +1081,10 @@ static int select_launch(int op, KeyXform xf, void *keys, void *vals, uint64_t *
     // of the bucket lie in the other side's region: copying the array to
     // scratch during round 0's read and writing every key once from the copy
     // costs less than listing and moving the misplaced ones (qselect float32
-    // 2^27, k = 2^26: 0.76 against 1.38 ms with a copy-back of the outer
-    // regions after the split, which the copy during round 0 replaced).  Within n / 4096 of an end only a few keys are
-    // recorded, and the sparse in-place split reads the array at little more
-    // than memory speed.
+    // 2^27, k = 2^26: 0.60 ms; 0.76 against 1.38 ms with a copy-back of the
+    // outer regions after the split, which the copy during round 0 replaced).
+    // Within n / 4096 of an end only a few keys are recorded, and the sparse
+    // in-place split reads the array at little more than memory speed.
     const bool out_of_place = std::min(k, n - 1 - k) >= n / 4096;
     for (int r = 0; r < rounds; ++r) {
         const int hi = W - SEL_DIGIT * r;
